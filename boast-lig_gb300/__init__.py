@@ -1,0 +1,208 @@
+"""libconv-gb300 host side: ctypes binding of the sm_103a C-ABI library.
+
+The binding mirrors how the reference drives its generated kernels: a BOAST
+``CKernel`` is run as ``k.run(*args)`` with the procedure's own argument list
+and returns a stats hash ``{:duration, :reference_return}``
+(BOAST runtime, called e.g. at BigDFT/MagicFilter1d2.rb:55-58 and
+BigDFT/Kinetic1d-nb.ipynb cells 15-16).  ``Kernel(name).run(...)`` here takes
+the same arguments in the same order (numpy arrays in place of NArrays) and
+returns ``{'duration': seconds, 'reference_return': {...}}``; a non-zero status
+raises ``LibconvError``.  ``run_dev`` is the device-pointer form (torch CUDA
+tensors or raw integer addresses plus an optional stream).
+
+There is no CPU fallback: if the CUDA library is missing the import of the
+kernel fails loudly.
+"""
+import ctypes
+import os
+import re
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, 'libconv_gb300.so')
+HEADER = os.path.join(HERE, '..', 'include', 'libconv_gb300.h')
+
+BC_SHRINK, BC_PERIODIC, BC_GROW, BC_FREE = -1, 0, 1, 2
+MODE_FP64 = 0
+
+_I = ctypes.POINTER(ctypes.c_int)
+_D = ctypes.POINTER(ctypes.c_double)
+_L = ctypes.POINTER(ctypes.c_longlong)
+_int, _dbl, _vp = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+
+_CONV1D = [_int, _int, _I, _int, _I, _I, _int, _vp, _vp, _dbl, _dbl, _dbl]
+_WAV1D = [_int, _int, _I, _int, _I, _I, _int, _vp, _vp, _dbl, _dbl]
+_MDT = [_int, _I, _I, _I, _I, _int, _vp, _vp, _vp, _vp]
+_WMD = [_int, _I, _I, _vp, _vp, _vp, _vp]
+_KIN = [_int, _I, _I, _vp, _vp, _vp, _vp, _D, _dbl, _dbl]
+
+SIGNATURES = {
+    'd_s0s0_1d_sym8_md': _CONV1D, 'd_s0s0_1d_sym8_imd': _CONV1D, 'd_s0s0_1d_sym8_d1': _CONV1D,
+    'd_s0s0_1d_sym8_d2_dotin': _CONV1D + [_vp],
+    'd_s0s1_1d_sym8': _WAV1D, 'd_s1s0_1d_sym8': _WAV1D,
+    'd_s0s1_1d_symicomb8': _WAV1D, 'd_s1s0_1d_symicomb8': _WAV1D,
+    'd_sfrf_ld_narr': _MDT, 'd_rfsf_ld_narr': _MDT,
+    'd_kin': _KIN, 'd_dwt_sym8': _WMD, 'd_idwt_sym8': _WMD,
+}
+COST_SIGNATURES = {
+    'd_s0s0_1d_sym8_md_cost': [_int, _int, _I, _int, _int, _L],
+    'd_s0s0_1d_sym8_d2_cost': [_int, _int, _I, _int, _int, _L],
+    'd_s0s1_1d_sym8_cost': [_int, _int, _I, _int, _int, _L],
+    'd_sfrf_cost': [_int, _I, _I, _int, _L],
+    'd_kin_cost': [_int, _I, _I, _L],
+    'd_dwt_sym8_cost': [_int, _I, _I, _L],
+}
+
+_lib = None
+
+
+class LibconvError(RuntimeError):
+    def __init__(self, status, name, detail):
+        super().__init__(f"{name} returned {status}: {detail}")
+        self.status = status
+
+
+def lib():
+    """The loaded CUDA library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in SIGNATURES.items():
+            for suffix, extra in (('', []), ('_dev', [_vp])):
+                fn = getattr(L, name + suffix)
+                fn.argtypes = args + extra
+                fn.restype = _int
+        for name, args in COST_SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = _int
+        for name in ('libconv_gb300_version', 'libconv_gb300_strerror', 'libconv_gb300_last_error'):
+            getattr(L, name).restype = ctypes.c_char_p
+        L.libconv_gb300_strerror.argtypes = [_int]
+        L.libconv_gb300_set_mode.argtypes = [_int]
+        L.libconv_gb300_set_mode.restype = _int
+        L.libconv_gb300_get_mode.restype = _int
+        _lib = L
+    return _lib
+
+
+def declared_symbols():
+    """Every function name declared in include/libconv_gb300.h."""
+    text = open(HEADER).read()
+    text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
+    return sorted(set(re.findall(r'\b(?:int|const char \*|void)\s*\**\s*(\w+)\s*\(', text)))
+
+
+def last_error():
+    return lib().libconv_gb300_last_error().decode()
+
+
+def set_mode(mode):
+    st = lib().libconv_gb300_set_mode(int(mode))
+    if st:
+        raise LibconvError(st, 'libconv_gb300_set_mode', last_error())
+
+
+def _ints(v):
+    if v is None:
+        return None
+    v = [int(t) for t in (v if hasattr(v, '__len__') else [v])]
+    return (ctypes.c_int * len(v))(*v)
+
+
+def _host_ptr(a, writable):
+    if a is None:
+        return None
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64:
+        raise TypeError('host arrays must be numpy float64')
+    if not (a.flags.c_contiguous or a.flags.f_contiguous):
+        raise TypeError('host arrays must be contiguous')
+    if writable and not a.flags.writeable:
+        raise TypeError('output array is read-only')
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _dev_ptr(t):
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return ctypes.c_void_p(t)
+    if hasattr(t, 'data_ptr'):
+        if not t.is_cuda or str(t.dtype) != 'torch.float64' or not t.is_contiguous():
+            raise TypeError('device arrays must be contiguous float64 CUDA tensors')
+        return ctypes.c_void_p(t.data_ptr())
+    raise TypeError(f'unsupported device array {type(t)}')
+
+
+class Kernel:
+    """One exported procedure, run the way BOAST runs a generated kernel."""
+
+    def __init__(self, name):
+        if name not in SIGNATURES:
+            raise KeyError(name)
+        self.name = name
+        self.argtypes = SIGNATURES[name]
+        L = lib()
+        self._host = getattr(L, name)
+        self._dev = getattr(L, name + '_dev')
+
+    def _convert(self, args, ptr):
+        if len(args) != len(self.argtypes):
+            raise TypeError(f"{self.name} takes {len(self.argtypes)} arguments, got {len(args)}")
+        out, dot = [], None
+        for i, (a, t) in enumerate(zip(args, self.argtypes)):
+            if t is _I:
+                out.append(_ints(a))
+            elif t is _D:
+                vals = [float(v) for v in a]
+                out.append(ctypes.cast((ctypes.c_double * len(vals))(*vals), _D))
+            elif t is _vp:
+                if self.name.endswith('dotin') and i == len(self.argtypes) - 1:
+                    dot = a
+                    out.append(None)
+                else:
+                    out.append(ptr(a))
+            else:
+                out.append(a)
+        return out, dot
+
+    def run(self, *args):
+        """Host-pointer call; returns {'duration', 'reference_return'}."""
+        conv, _ = self._convert(args, lambda a: _host_ptr(a, True))
+        dot = ctypes.c_double(0.0)
+        if self.name.endswith('dotin'):
+            conv[-1] = ctypes.cast(ctypes.pointer(dot), ctypes.c_void_p)
+        t0 = time.perf_counter()
+        st = self._host(*conv)
+        dt = time.perf_counter() - t0
+        if st:
+            raise LibconvError(st, self.name, last_error())
+        ret = {'dot_in': dot.value} if self.name.endswith('dotin') else {}
+        return {'duration': dt, 'reference_return': ret}
+
+    def run_dev(self, *args, stream=None):
+        """Device-pointer call (enqueue only); dot_in is a device pointer."""
+        conv, dot = self._convert(args, _dev_ptr)
+        if self.name.endswith('dotin'):
+            conv[-1] = _dev_ptr(dot)
+        s = stream
+        if s is not None and not isinstance(s, int):
+            s = s.cuda_stream if hasattr(s, 'cuda_stream') else int(s)
+        st = self._dev(*conv, ctypes.c_void_p(s) if s else None)
+        if st:
+            raise LibconvError(st, self.name + '_dev', last_error())
+
+
+def cost(name, *args):
+    """Reference flop model of an operator (``<name>_cost`` export)."""
+    fn = getattr(lib(), name)
+    out = ctypes.c_longlong(0)
+    conv = [(_ints(a) if t is _I else a) for a, t in zip(args, fn.argtypes[:-1])]
+    st = fn(*conv, ctypes.byref(out))
+    if st:
+        raise LibconvError(st, name, last_error())
+    return out.value

@@ -1,0 +1,43 @@
+// One 1D sweep of a separable convolution over a batch of lines: the unit of
+// work every entry point of the library is decomposed into.  Semantics are
+// those of one generated ConvolutionOperator1d call
+// (BigDFT/GenericConvolution2.rb:1036-1442), applied to `narr` arrays.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lcg {
+
+enum Kind { KCONV = 0, KDEC = 1, KREC = 2 };
+enum Bc { BC_SHRINK = -1, BC_PERIODIC = 0, BC_GROW = 1, BC_FREE = 2 };
+
+struct Sweep {
+    int kind;            // KCONV (1 channel), KDEC (s0s1), KREC (s1s0)
+    int ntaps;           // taps (polyphase taps for wavelets)
+    int lowfil;          // first tap offset
+    int bc;
+    int ftab;            // offset of the filter in the device filter table
+    int nL, n, nR;       // lines = nL*nR; n = processed size (pairs for wavelets)
+    int in_lo, in_ext;   // input processed-dim index range [in_lo, in_lo+in_ext)
+    int out_lo, out_ext; // output processed-dim index range
+    int qlo, qhi;        // outputs computed: q in [qlo, qhi]
+    int transpose;       // 1: y(line, q) (rotated), only with nL == 1
+    int narr;
+    long long x_arr, y_arr;   // element stride between the narr arrays
+    const double *x;
+    const double *x2;         // kinetic partial sum added to the output (or null)
+    double *y;
+    int has_a, has_ax, ay_mode, has_dot;   // ay_mode: 0 write, 1 a_y*y+out, 2 y+out
+    double a, a_x, a_y;
+    double *dot_part;         // one partial per block (device), when has_dot
+};
+
+// Number of dot partials the FP64 sweep writes for S (grid size).
+long long sweep_fp64_blocks(const Sweep &S);
+// Enqueue the FP64 SIMT sweep on `st`.
+cudaError_t launch_sweep_fp64(const Sweep &S, cudaStream_t st);
+// Deterministic sum of `count` partials into *out (device), on `st`.
+cudaError_t launch_dot_reduce(const double *part, long long count, double *out, int accumulate,
+                              cudaStream_t st);
+
+}  // namespace lcg

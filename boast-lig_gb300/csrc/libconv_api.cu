@@ -1,0 +1,576 @@
+// C-ABI of libconv-gb300: the generated libconv dispatchers restated as
+// plans of 1D sweeps (lcg::Sweep) launched on the GPU.
+//
+//  - 1D entry points follow GenericConvolutionOperator1d#procedure
+//    (BigDFT/GenericConvolution2.rb:1560-1764);
+//  - multi-D entry points follow GenericConvolutionOperator#procedure
+//    (BigDFT/GenericConvolution2.rb:1934-2243) for transpose = 1
+//    (MagicFilter, wavelets) and transpose = 0 with the kinetic options.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/libconv_gb300.h"
+#include "lcg_sweep.cuh"
+#include "libconv_filters.h"
+
+using namespace lcg;
+
+namespace {
+
+thread_local std::string t_err;
+thread_local int t_mode = LIBCONV_MODE_FP64;
+
+int fail(int code, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    t_err = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    return fail(LIBCONV_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// ---- operator definitions ---------------------------------------------------
+struct OpDef {
+    int kind;
+    int ftab[2], ntaps[2], lowfil[2];   // [0]: periodic/free filters, [1]: grow/shrink
+    int length;                         // filter.length (cost model, grow extents)
+    int cost_per_out;                   // filter.cost (GenericConvolution2.rb:231-233, 499-501)
+};
+
+#define CONV_OP(TAB, NT, LOW) { KCONV, {TAB, TAB}, {NT, NT}, {LOW, LOW}, NT, 2 * NT }
+#define WT_OP(KIND, P, GS) { KIND, {LCG_FTAB_##P, LCG_FTAB_##GS}, {LCG_##P##_NTAPS, LCG_##GS##_NTAPS}, \
+        {LCG_##P##_LOWFIL, LCG_##GS##_LOWFIL}, LCG_##P##_LENGTH, 4 * LCG_##P##_LENGTH }
+
+const OpDef OP_MD = CONV_OP(LCG_FTAB_MD, 16, LCG_CONV_SYM8_MD_LOWFIL);
+const OpDef OP_IMD = CONV_OP(LCG_FTAB_IMD, 16, LCG_CONV_SYM8_IMD_LOWFIL);
+const OpDef OP_D1 = CONV_OP(LCG_FTAB_D1, 29, LCG_CONV_SYM8_D1_LOWFIL);
+const OpDef OP_D2 = CONV_OP(LCG_FTAB_D2, 29, LCG_CONV_SYM8_D2_LOWFIL);
+const OpDef OP_DWT = WT_OP(KDEC, WT_SYM8_DEC_P, WT_SYM8_DEC_GS);
+const OpDef OP_IWT = WT_OP(KREC, WT_SYM8_REC_P, WT_SYM8_REC_GS);
+const OpDef OP_RTOS1 = WT_OP(KDEC, WT_SYMICOMB8_DEC_P, WT_SYMICOMB8_DEC_GS);
+const OpDef OP_S1TOR = WT_OP(KREC, WT_SYMICOMB8_REC_P, WT_SYMICOMB8_REC_GS);
+
+bool bc_valid(int bc) {
+    return bc == BC_PERIODIC || bc == BC_GROW || bc == BC_SHRINK || bc == BC_FREE;
+}
+int fam(int bc) { return (bc == BC_GROW || bc == BC_SHRINK) ? 1 : 0; }
+int nch(const OpDef &op) { return op.kind == KCONV ? 1 : 2; }
+// processed-dim extents needed (positions; pairs for wavelets)
+int need_in(const OpDef &op, int bc, int n) { return bc == BC_SHRINK ? n + op.ntaps[1] - 1 : n; }
+int need_out(const OpDef &op, int bc, int n) { return bc == BC_GROW ? n + op.ntaps[1] - 1 : n; }
+
+// Fill the geometry of a sweep (GenericConvolution2.rb:61-85, 206-225, 1009-1022).
+void geometry(const OpDef &op, int bc, int nL, int n, int nR, int ld_in, int ld_out, Sweep &S) {
+    const int f = fam(bc);
+    S.kind = op.kind;
+    S.ntaps = op.ntaps[f];
+    S.lowfil = op.lowfil[f];
+    S.ftab = op.ftab[f];
+    S.bc = bc;
+    S.nL = nL; S.n = n; S.nR = nR;
+    const int up = S.lowfil + S.ntaps - 1;
+    S.in_lo = bc == BC_SHRINK ? S.lowfil : 0;
+    S.in_ext = ld_in;
+    S.out_lo = bc == BC_GROW ? -up : 0;
+    S.out_ext = ld_out;
+    S.qlo = bc == BC_GROW ? -up : 0;
+    S.qhi = bc == BC_GROW ? n - S.lowfil - 1 : n - 1;
+    S.transpose = 0;
+    S.narr = 1;
+    S.x_arr = S.y_arr = 0;
+    S.x = S.x2 = nullptr;
+    S.y = nullptr;
+    S.has_a = S.has_ax = S.ay_mode = S.has_dot = 0;
+    S.a = 1.0; S.a_x = 0.0; S.a_y = 0.0;
+    S.dot_part = nullptr;
+}
+
+// ---- per-device resources ------------------------------------------------------
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+};
+
+struct DevState {
+    bool init = false;
+    cudaStream_t stream = nullptr;   // stream of the host-pointer entry points
+    DevBuf buf[6];                   // x, y, w1, w2, dot partials, dot scalar
+    DevBuf scratch;                  // dot partials of the *_dev entry points
+    DevBuf dscalar;
+};
+
+std::mutex g_mu;
+DevState g_dev[64];
+
+int current_device(int &dev) {
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= 64) return fail(LIBCONV_ECUDA, "device index %d out of range", dev);
+    return LIBCONV_OK;
+}
+
+int ensure(DevBuf &b, size_t bytes) {
+    if (b.cap >= bytes) return LIBCONV_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+    size_t want = bytes < 256 ? 256 : bytes;
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(LIBCONV_ENOMEM, "cudaMalloc(%zu bytes): %s", want, cudaGetErrorString(e));
+    }
+    b.cap = want;
+    return LIBCONV_OK;
+}
+
+DevState *dev_state(int &rc) {
+    int dev;
+    rc = current_device(dev);
+    if (rc) return nullptr;
+    DevState &s = g_dev[dev];
+    if (!s.init) {
+        cudaError_t e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { rc = cuda_fail(e, "cudaStreamCreate"); return nullptr; }
+        s.init = true;
+    }
+    return &s;
+}
+
+// ---- plans -------------------------------------------------------------------
+enum BufId { B_X = 0, B_Y = 1, B_W1 = 2, B_W2 = 3 };
+
+struct PlanStep {
+    Sweep S;
+    int src, dst, src2;   // buffer ids (src2 = -1 if no x2)
+};
+
+struct Plan {
+    std::vector<PlanStep> steps;
+    size_t elems[4] = {0, 0, 0, 0};   // elements each buffer must hold
+    size_t y_read = 0;                // y is read (a_y != 0)
+    int has_dot = 0;
+};
+
+void need(Plan &P, int b, size_t e) { if (P.elems[b] < e) P.elems[b] = e; }
+
+// 1D dispatcher (GenericConvolution2.rb:1560-1764).
+int plan_1d(const OpDef &op, int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+            int narr, double a, int use_ax, double a_x, double a_y, int dot, Plan &P) {
+    if (d < 1 || idim < 0 || idim >= d) return fail(LIBCONV_EARG, "d=%d idim=%d", d, idim);
+    if (!n || !nx || !ny) return fail(LIBCONV_EARG, "n/nx/ny must not be null");
+    if (narr < 1 || narr > 65535) return fail(LIBCONV_EARG, "narr=%d out of [1,65535]", narr);
+    if (!bc_valid(bc)) return fail(LIBCONV_EBC, "unknown boundary condition %d", bc);
+    for (int i = 0; i < d; ++i)
+        if (n[i] < 1 || nx[i] < 1 || ny[i] < 1)
+            return fail(LIBCONV_EARG, "n/nx/ny[%d] must be >= 1", i);
+    if (nx[idim] < need_in(op, bc, n[idim]) || ny[idim] < need_out(op, bc, n[idim]))
+        return fail(LIBCONV_ESIZE, "nx[%d]=%d / ny[%d]=%d too small for n=%d bc=%d", idim, nx[idim],
+                    idim, ny[idim], n[idim], bc);
+    const long long m = nch(op);
+    long long nL = 1, nR = 1;
+    for (int i = 0; i < idim; ++i) nL *= nx[i] * m;
+    for (int i = idim + 1; i < d; ++i) nR *= nx[i] * m;
+    if (nL * nR > (1LL << 31) - 1) return fail(LIBCONV_EARG, "too many lines");
+    PlanStep st;
+    geometry(op, bc, (int)nL, n[idim], (int)nR, nx[idim], ny[idim], st.S);
+    st.S.narr = narr;
+    st.S.x_arr = (long long)nx[idim] * m * nL * nR;
+    st.S.y_arr = (long long)ny[idim] * m * nL * nR;
+    st.S.has_a = a != 1.0;
+    st.S.a = a;
+    st.S.has_ax = use_ax && a_x != 0.0;
+    st.S.a_x = a_x;
+    st.S.ay_mode = a_y != 0.0 ? 1 : 0;
+    st.S.a_y = a_y;
+    st.S.has_dot = dot;
+    st.src = B_X; st.dst = B_Y; st.src2 = -1;
+    P.steps.push_back(st);
+    need(P, B_X, st.S.x_arr * narr);
+    need(P, B_Y, st.S.y_arr * narr);
+    P.y_read = st.S.ay_mode ? st.S.y_arr * narr : 0;
+    // ld padding past the computed outputs is left untouched, as the
+    // generated loops do: host callers get their padding back unchanged
+    if (ny[idim] > need_out(op, bc, n[idim])) P.y_read = st.S.y_arr * narr;
+    P.has_dot = dot;
+    return LIBCONV_OK;
+}
+
+// Ping-pong of the multi-D dispatcher (GenericConvolution2.rb:2155-2240):
+// sweep 0 x->w1, odd middle sweeps w1->w2, even ones w2->w1, last ->y.
+void pingpong(int d, int i, int &src, int &dst) {
+    if (d == 1) { src = B_X; dst = B_Y; return; }
+    if (i == 0) { src = B_X; dst = B_W1; return; }
+    if (i == d - 1) { src = ((d - 1) % 2 == 1) ? B_W1 : B_W2; dst = B_Y; return; }
+    src = (i % 2 == 1) ? B_W1 : B_W2;
+    dst = (i % 2 == 1) ? B_W2 : B_W1;
+}
+
+// Multi-D, transpose = 1 (MagicFilter, wavelets).
+int plan_md_t(const OpDef &op, int d, const int *n, const int *bc, const int *nx, const int *ny,
+              int narr, Plan &P) {
+    if (d < 1 || d > 16) return fail(LIBCONV_EARG, "d=%d out of [1,16]", d);
+    if (!n || !bc) return fail(LIBCONV_EARG, "n/bc must not be null");
+    if (narr < 1 || narr > 65535) return fail(LIBCONV_EARG, "narr=%d out of [1,65535]", narr);
+    const bool ld = nx != nullptr;
+    if (ld && !ny) return fail(LIBCONV_EARG, "ny must not be null when nx is given");
+    const long long m = nch(op);
+    long long dims[16];
+    for (int i = 0; i < d; ++i) {
+        if (n[i] < 1) return fail(LIBCONV_EARG, "n[%d]=%d", i, n[i]);
+        if (!bc_valid(bc[i])) return fail(LIBCONV_EBC, "unknown boundary condition %d", bc[i]);
+        if (ld) {
+            if (nx[i] < need_in(op, bc[i], n[i]) || ny[i] < need_out(op, bc[i], n[i]))
+                return fail(LIBCONV_ESIZE, "nx[%d]=%d / ny[%d]=%d too small for n=%d bc=%d", i,
+                            nx[i], i, ny[i], n[i], bc[i]);
+            dims[i] = nx[i] * m;
+        } else {
+            dims[i] = need_in(op, bc[i], n[i]) * m;
+        }
+    }
+    for (int i = 0; i < d; ++i) {
+        long long ndat = 1;
+        for (int j = 0; j < d; ++j) if (j != i) ndat *= dims[j];
+        if (ndat > (1LL << 31) - 1) return fail(LIBCONV_EARG, "too many lines");
+        const int in_ext = (int)(dims[i] / m);
+        const int out_ext = ld ? ny[i] : need_out(op, bc[i], n[i]);
+        PlanStep st;
+        geometry(op, bc[i], 1, n[i], (int)ndat, in_ext, out_ext, st.S);
+        st.S.transpose = 1;
+        st.S.narr = narr;
+        st.S.x_arr = ndat * dims[i];
+        st.S.y_arr = ndat * out_ext * m;
+        pingpong(d, i, st.src, st.dst);
+        st.src2 = -1;
+        need(P, st.src, st.S.x_arr * narr);
+        need(P, st.dst, st.S.y_arr * narr);
+        P.steps.push_back(st);
+        dims[i] = out_ext * m;
+        if (i == d - 1 && out_ext > need_out(op, bc[i], n[i])) P.y_read = st.S.y_arr * narr;
+    }
+    return LIBCONV_OK;
+}
+
+// Multi-D kinetic, transpose = 0 (Kinetic2.rb:1068-1090).
+int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, double a_y,
+             Plan &P) {
+    if (d < 1 || d > 16) return fail(LIBCONV_EARG, "d=%d out of [1,16]", d);
+    if (!n || !bc || !a) return fail(LIBCONV_EARG, "n/bc/a must not be null");
+    long long tot = 1;
+    for (int i = 0; i < d; ++i) {
+        if (n[i] < 1) return fail(LIBCONV_EARG, "n[%d]=%d", i, n[i]);
+        if (bc[i] != BC_PERIODIC && bc[i] != BC_FREE)
+            return fail(LIBCONV_EBC, "kinetic supports periodic and free (no-grow) only, bc[%d]=%d",
+                        i, bc[i]);
+        tot *= n[i];
+    }
+    if (tot > (1LL << 31) - 1) return fail(LIBCONV_EARG, "grid too large");
+    for (int i = 0; i < d; ++i) {
+        long long nL = 1, nR = 1;
+        for (int j = 0; j < i; ++j) nL *= n[j];
+        for (int j = i + 1; j < d; ++j) nR *= n[j];
+        PlanStep st;
+        geometry(OP_D2, bc[i], (int)nL, n[i], (int)nR, n[i], n[i], st.S);
+        const bool last = i == d - 1;
+        st.S.has_a = 1;
+        st.S.a = a[i];
+        st.S.has_ax = i == 0;
+        st.S.a_x = a_x;
+        st.S.ay_mode = (last && a_y != 0.0) ? 1 : 0;
+        st.S.a_y = a_y;
+        int s, t;
+        pingpong(d, i, s, t);
+        st.src = B_X;
+        st.dst = t;
+        st.src2 = i == 0 ? -1 : s;
+        need(P, B_X, tot);
+        need(P, t, tot);
+        if (st.src2 >= 0) need(P, st.src2, tot);
+        P.steps.push_back(st);
+    }
+    P.y_read = a_y != 0.0 ? tot : 0;
+    return LIBCONV_OK;
+}
+
+// ---- execution ------------------------------------------------------------------
+// Launch the plan's sweeps with bound device pointers.  dot_dev receives the
+// dot product (device) when the plan has one; `scratch` holds the partials.
+int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, double *dot_dev,
+             cudaStream_t st) {
+    if (t_mode != LIBCONV_MODE_FP64) return fail(LIBCONV_EMODE, "unknown mode %d", t_mode);
+    for (const PlanStep &ps : P.steps) {
+        Sweep S = ps.S;
+        S.x = bufs[ps.src];
+        S.y = bufs[ps.dst];
+        S.x2 = ps.src2 >= 0 ? bufs[ps.src2] : nullptr;
+        if (!S.x || !S.y || (ps.src2 >= 0 && !S.x2))
+            return fail(LIBCONV_EARG, "null device buffer in plan");
+        long long nb = 0;
+        if (S.has_dot) {
+            nb = sweep_fp64_blocks(S);
+            int rc = ensure(scratch, (size_t)nb * sizeof(double));
+            if (rc) return rc;
+            S.dot_part = (double *)scratch.p;
+        }
+        cudaError_t e = launch_sweep_fp64(S, st);
+        if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
+        if (S.has_dot) {
+            e = launch_dot_reduce(S.dot_part, nb, dot_dev, 0, st);
+            if (e != cudaSuccess) return cuda_fail(e, "dot reduction launch");
+        }
+    }
+    return LIBCONV_OK;
+}
+
+// Device-pointer execution (caller-owned buffers, no host synchronisation).
+int exec_dev(const Plan &P, const double *x, double *y, double *w1, double *w2, double *dot_dev,
+             void *stream) {
+    if (!x || !y) return fail(LIBCONV_EARG, "x/y must not be null");
+    if (P.elems[B_W1] && !w1) return fail(LIBCONV_EARG, "w1 workspace required");
+    if (P.elems[B_W2] && !w2) return fail(LIBCONV_EARG, "w2 workspace required");
+    if (P.has_dot && !dot_dev) return fail(LIBCONV_EARG, "dot_in must not be null");
+    double *bufs[4] = {const_cast<double *>(x), y, w1, w2};
+    std::lock_guard<std::mutex> lk(g_mu);
+    int rc;
+    DevState *s = dev_state(rc);
+    if (!s) return rc;
+    return run_plan(P, bufs, s->scratch, dot_dev, (cudaStream_t)stream);
+}
+
+// Host-pointer execution: stage in device buffers owned by the library.
+int exec_host(const Plan &P, const double *x, double *y, double *dot_host) {
+    if (!x || !y) return fail(LIBCONV_EARG, "x/y must not be null");
+    if (P.has_dot && !dot_host) return fail(LIBCONV_EARG, "dot_in must not be null");
+    std::lock_guard<std::mutex> lk(g_mu);
+    int rc;
+    DevState *s = dev_state(rc);
+    if (!s) return rc;
+    for (int b = 0; b < 4; ++b)
+        if (P.elems[b] && (rc = ensure(s->buf[b], P.elems[b] * sizeof(double)))) return rc;
+    if (P.has_dot && (rc = ensure(s->dscalar, sizeof(double)))) return rc;
+    double *bufs[4];
+    for (int b = 0; b < 4; ++b) bufs[b] = P.elems[b] ? (double *)s->buf[b].p : nullptr;
+    cudaStream_t st = s->stream;
+    cudaError_t e = cudaMemcpyAsync(bufs[B_X], x, P.elems[B_X] * sizeof(double),
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "copy x to device");
+    if (P.y_read) {
+        e = cudaMemcpyAsync(bufs[B_Y], y, P.y_read * sizeof(double), cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(e, "copy y to device");
+    }
+    rc = run_plan(P, bufs, s->scratch, P.has_dot ? (double *)s->dscalar.p : nullptr, st);
+    if (rc) return rc;
+    e = cudaMemcpyAsync(y, bufs[B_Y], P.elems[B_Y] * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return cuda_fail(e, "copy y to host");
+    if (P.has_dot) {
+        e = cudaMemcpyAsync(dot_host, s->dscalar.p, sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return cuda_fail(e, "copy dot_in to host");
+    }
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "synchronize");
+    return LIBCONV_OK;
+}
+
+// ---- cost model (GenericConvolution2.rb:1269-1276, 1525-1558, 1850-1932) ----
+int cost_1d(const OpDef &op, int d, int idim, const int *n, int bc, int narr, long long *cost) {
+    if (!cost || !n || d < 1 || idim < 0 || idim >= d || narr < 1)
+        return fail(LIBCONV_EARG, "bad cost arguments");
+    if (!bc_valid(bc)) return fail(LIBCONV_EBC, "unknown boundary condition %d", bc);
+    long long ndat = 1;
+    for (int i = 0; i < d; ++i) if (i != idim) ndat *= n[i];
+    *cost = (long long)n[idim] * op.cost_per_out * ndat * narr;
+    return LIBCONV_OK;
+}
+
+int cost_md(const OpDef &op, int d, const int *n, const int *bc, int narr, long long *cost) {
+    if (!cost || !n || !bc || d < 1 || d > 16 || narr < 1) return fail(LIBCONV_EARG, "bad cost arguments");
+    const int m = nch(op);
+    const int L = op.length;
+    long long dims[16];
+    for (int i = 0; i < d; ++i) {
+        if (!bc_valid(bc[i])) return fail(LIBCONV_EBC, "unknown boundary condition %d", bc[i]);
+        if (bc[i] == BC_SHRINK) dims[i] = m == 2 ? 2LL * n[i] + L - 2 : n[i] + L - 1;
+        else dims[i] = (long long)m * n[i];
+    }
+    long long c = 0;
+    for (int i = 0; i < d; ++i) {
+        long long ndat = 1;
+        for (int j = 0; j < d; ++j) if (j != i) ndat *= dims[j];
+        c += (long long)n[i] * op.cost_per_out * ndat;
+        if (bc[i] == BC_GROW) dims[i] = m == 2 ? 2LL * n[i] + L - 2 : n[i] + L - 1;
+        else dims[i] = (long long)m * n[i];
+    }
+    *cost = c * narr;
+    return LIBCONV_OK;
+}
+
+}  // namespace
+
+// =============================== exported C ABI ===============================
+extern "C" {
+
+const char *libconv_gb300_version(void) { return "libconv-gb300 0.1 (sm_103a)"; }
+
+const char *libconv_gb300_strerror(int s) {
+    switch (s) {
+    case LIBCONV_OK: return "ok";
+    case LIBCONV_EARG: return "invalid argument";
+    case LIBCONV_EBC: return "unsupported boundary condition";
+    case LIBCONV_ESIZE: return "leading dimension too small";
+    case LIBCONV_ECUDA: return "CUDA error";
+    case LIBCONV_ENOMEM: return "device allocation failed";
+    case LIBCONV_EMODE: return "unknown compute mode";
+    default: return "unknown status";
+    }
+}
+
+const char *libconv_gb300_last_error(void) { return t_err.c_str(); }
+
+int libconv_gb300_set_mode(int mode) {
+    if (mode != LIBCONV_MODE_FP64) return fail(LIBCONV_EMODE, "unknown mode %d", mode);
+    t_mode = mode;
+    return LIBCONV_OK;
+}
+int libconv_gb300_get_mode(void) { return t_mode; }
+
+#define LCG_CONV1D(NAME, OP)                                                                     \
+    int NAME(int d, int idim, const int *n, int bc, const int *nx, const int *ny, int narr,     \
+             const double *x, double *y, double a, double a_x, double a_y) {                    \
+        Plan P;                                                                                 \
+        int rc = plan_1d(OP, d, idim, n, bc, nx, ny, narr, a, 1, a_x, a_y, 0, P);               \
+        return rc ? rc : exec_host(P, x, y, nullptr);                                           \
+    }                                                                                           \
+    int NAME##_dev(int d, int idim, const int *n, int bc, const int *nx, const int *ny, int narr, \
+                   const double *x, double *y, double a, double a_x, double a_y, void *stream) { \
+        Plan P;                                                                                 \
+        int rc = plan_1d(OP, d, idim, n, bc, nx, ny, narr, a, 1, a_x, a_y, 0, P);               \
+        return rc ? rc : exec_dev(P, x, y, nullptr, nullptr, nullptr, stream);                  \
+    }
+
+LCG_CONV1D(d_s0s0_1d_sym8_md, OP_MD)
+LCG_CONV1D(d_s0s0_1d_sym8_imd, OP_IMD)
+LCG_CONV1D(d_s0s0_1d_sym8_d1, OP_D1)
+
+int d_s0s0_1d_sym8_d2_dotin(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                            int narr, const double *x, double *y, double a, double a_x,
+                            double a_y, double *dot_in) {
+    Plan P;
+    int rc = plan_1d(OP_D2, d, idim, n, bc, nx, ny, narr, a, 1, a_x, a_y, 1, P);
+    return rc ? rc : exec_host(P, x, y, dot_in);
+}
+int d_s0s0_1d_sym8_d2_dotin_dev(int d, int idim, const int *n, int bc, const int *nx,
+                                const int *ny, int narr, const double *x, double *y, double a,
+                                double a_x, double a_y, double *dot_in, void *stream) {
+    Plan P;
+    int rc = plan_1d(OP_D2, d, idim, n, bc, nx, ny, narr, a, 1, a_x, a_y, 1, P);
+    return rc ? rc : exec_dev(P, x, y, nullptr, nullptr, dot_in, stream);
+}
+
+#define LCG_WAV1D(NAME, OP)                                                                      \
+    int NAME(int d, int idim, const int *n, int bc, const int *nx, const int *ny, int narr,     \
+             const double *x, double *y, double a, double a_y) {                                \
+        Plan P;                                                                                 \
+        int rc = plan_1d(OP, d, idim, n, bc, nx, ny, narr, a, 0, 0.0, a_y, 0, P);               \
+        return rc ? rc : exec_host(P, x, y, nullptr);                                           \
+    }                                                                                           \
+    int NAME##_dev(int d, int idim, const int *n, int bc, const int *nx, const int *ny, int narr, \
+                   const double *x, double *y, double a, double a_y, void *stream) {            \
+        Plan P;                                                                                 \
+        int rc = plan_1d(OP, d, idim, n, bc, nx, ny, narr, a, 0, 0.0, a_y, 0, P);               \
+        return rc ? rc : exec_dev(P, x, y, nullptr, nullptr, nullptr, stream);                  \
+    }
+
+LCG_WAV1D(d_s0s1_1d_sym8, OP_DWT)
+LCG_WAV1D(d_s1s0_1d_sym8, OP_IWT)
+LCG_WAV1D(d_s0s1_1d_symicomb8, OP_RTOS1)
+LCG_WAV1D(d_s1s0_1d_symicomb8, OP_S1TOR)
+
+#define LCG_MDT(NAME, OP)                                                                        \
+    int NAME(int d, const int *n, const int *bc, const int *nx, const int *ny, int narr,        \
+             const double *x, double *y, double *w1, double *w2) {                              \
+        (void)w1; (void)w2;                                                                     \
+        Plan P;                                                                                 \
+        int rc = plan_md_t(OP, d, n, bc, nx, ny, narr, P);                                      \
+        return rc ? rc : exec_host(P, x, y, nullptr);                                           \
+    }                                                                                           \
+    int NAME##_dev(int d, const int *n, const int *bc, const int *nx, const int *ny, int narr,  \
+                   const double *x, double *y, double *w1, double *w2, void *stream) {          \
+        Plan P;                                                                                 \
+        int rc = plan_md_t(OP, d, n, bc, nx, ny, narr, P);                                      \
+        return rc ? rc : exec_dev(P, x, y, w1, w2, nullptr, stream);                            \
+    }
+
+LCG_MDT(d_sfrf_ld_narr, OP_MD)
+LCG_MDT(d_rfsf_ld_narr, OP_IMD)
+
+int d_dwt_sym8(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
+               double *w2) {
+    (void)w1; (void)w2;
+    Plan P;
+    int rc = plan_md_t(OP_DWT, d, n, bc, nullptr, nullptr, 1, P);
+    return rc ? rc : exec_host(P, x, y, nullptr);
+}
+int d_idwt_sym8(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
+                double *w2) {
+    (void)w1; (void)w2;
+    Plan P;
+    int rc = plan_md_t(OP_IWT, d, n, bc, nullptr, nullptr, 1, P);
+    return rc ? rc : exec_host(P, x, y, nullptr);
+}
+int d_dwt_sym8_dev(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
+                   double *w2, void *stream) {
+    Plan P;
+    int rc = plan_md_t(OP_DWT, d, n, bc, nullptr, nullptr, 1, P);
+    return rc ? rc : exec_dev(P, x, y, w1, w2, nullptr, stream);
+}
+int d_idwt_sym8_dev(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
+                    double *w2, void *stream) {
+    Plan P;
+    int rc = plan_md_t(OP_IWT, d, n, bc, nullptr, nullptr, 1, P);
+    return rc ? rc : exec_dev(P, x, y, w1, w2, nullptr, stream);
+}
+
+int d_kin(int d, const int *n, const int *bc, const double *x, double *y, double *w1, double *w2,
+          const double *a, double a_x, double a_y) {
+    (void)w1; (void)w2;
+    Plan P;
+    int rc = plan_kin(d, n, bc, a, a_x, a_y, P);
+    return rc ? rc : exec_host(P, x, y, nullptr);
+}
+int d_kin_dev(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
+              double *w2, const double *a, double a_x, double a_y, void *stream) {
+    Plan P;
+    int rc = plan_kin(d, n, bc, a, a_x, a_y, P);
+    return rc ? rc : exec_dev(P, x, y, w1, w2, nullptr, stream);
+}
+
+int d_s0s0_1d_sym8_md_cost(int d, int idim, const int *n, int bc, int narr, long long *cost) {
+    return cost_1d(OP_MD, d, idim, n, bc, narr, cost);
+}
+int d_s0s0_1d_sym8_d2_cost(int d, int idim, const int *n, int bc, int narr, long long *cost) {
+    return cost_1d(OP_D2, d, idim, n, bc, narr, cost);
+}
+int d_s0s1_1d_sym8_cost(int d, int idim, const int *n, int bc, int narr, long long *cost) {
+    return cost_1d(OP_DWT, d, idim, n, bc, narr, cost);
+}
+int d_sfrf_cost(int d, const int *n, const int *bc, int narr, long long *cost) {
+    return cost_md(OP_MD, d, n, bc, narr, cost);
+}
+int d_kin_cost(int d, const int *n, const int *bc, long long *cost) {
+    return cost_md(OP_D2, d, n, bc, 1, cost);
+}
+int d_dwt_sym8_cost(int d, const int *n, const int *bc, long long *cost) {
+    return cost_md(OP_DWT, d, n, bc, 1, cost);
+}
+
+}  // extern "C"

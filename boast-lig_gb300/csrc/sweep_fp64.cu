@@ -1,0 +1,220 @@
+// FP64 SIMT sweep: the plain double-precision path.
+//
+// One CTA owns 32 lines x one chunk of QC outputs.  The input segment the
+// chunk needs (QC + taps - 1 positions, periodic wrap / free-boundary zero
+// fill / shrink offset applied at load time) is staged once in shared memory
+// with coalesced loads, then every output is a chain of FP64 FMAs in the
+// reference's tap order (lowfil..upfil).  Lanes map to lines, so the shared
+// reads are conflict-free and the stores of strided shapes and of the
+// rotated (transpose = 1) layout are coalesced.
+#include "lcg_sweep.cuh"
+#include "libconv_filters.h"
+
+namespace lcg {
+
+__constant__ double c_ftab[LCG_FTAB_N] = LCG_FTAB_INIT;
+
+namespace {
+
+constexpr int kLines = 32;
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kPad = kLines + 1;
+
+template <int KIND> struct Chunk { static constexpr int QC = KIND == KCONV ? 64 : 32; };
+
+__device__ __forceinline__ int imod(int a, int n) {
+    int r = a % n;
+    return r < 0 ? r + n : r;
+}
+
+// Input element of line g at logical processed index p (channel ch), with the
+// boundary condition applied; 0 outside the data of a free boundary.
+template <int KIND>
+__device__ __forceinline__ double fetch(const Sweep &S, const double *__restrict__ x, long long g,
+                                        int p, int ch, long long in_pext) {
+    int pos;
+    if (S.bc == BC_PERIODIC) {
+        pos = imod(p, S.n);
+    } else if (S.bc == BC_SHRINK) {
+        pos = p - S.in_lo;
+    } else {
+        if (p < 0 || p >= S.n) return 0.0;
+        pos = p;
+    }
+    const long long l = g % S.nL, r = g / S.nL;
+    const long long off = KIND == KDEC ? (long long)ch + 2LL * pos
+                                       : (long long)pos + (long long)S.in_ext * ch;
+    return x[l + (long long)S.nL * (off + in_pext * r)];
+}
+
+template <int KIND, int NT>
+__global__ void __launch_bounds__(kThreads) sweep_fp64_kernel(const Sweep S) {
+    constexpr int NCH = KIND == KCONV ? 1 : 2;
+    constexpr int QC = Chunk<KIND>::QC;
+    constexpr int SPAN = QC + NT - 1;
+    constexpr int NROW = SPAN * NCH;
+    __shared__ double tile[NROW * kPad];
+    __shared__ double red[kWarps];
+
+    const int arr = blockIdx.z;
+    const long long nlines = (long long)S.nL * S.nR;
+    const long long g0 = (long long)blockIdx.x * kLines;
+    const int qc0 = S.qlo + blockIdx.y * QC;
+    const int upfil = S.lowfil + NT - 1;
+    const int plast = S.qhi + upfil;  // last logical input index any output needs
+    const long long in_pext = (long long)S.in_ext * NCH;
+    const long long out_pext = (long long)S.out_ext * NCH;
+    const double *__restrict__ x = S.x + (long long)arr * S.x_arr;
+    double *__restrict__ y = S.y + (long long)arr * S.y_arr;
+    const double *__restrict__ x2 = S.x2 ? S.x2 + (long long)arr * S.x_arr : nullptr;
+
+    // ---- stage the input segment: row j*NCH+ch holds logical index qc0+lowfil+j
+    if (S.nL == 1) {
+        // positions fastest: consecutive threads read consecutive memory of one line
+        for (int idx = threadIdx.x; idx < NROW * kLines; idx += kThreads) {
+            int w, j, ch;
+            if (KIND == KREC) {          // blocked input: one channel block at a time
+                j = idx % SPAN; const int t = idx / SPAN; ch = t % NCH; w = t / NCH;
+            } else {                     // conv / interleaved input
+                const int k = idx % NROW; w = idx / NROW; j = k / NCH; ch = k % NCH;
+            }
+            const long long g = g0 + w;
+            const int p = qc0 + S.lowfil + j;
+            double v = 0.0;
+            if (g < nlines && p <= plast) v = fetch<KIND>(S, x, g, p, ch, in_pext);
+            tile[(j * NCH + ch) * kPad + w] = v;
+        }
+    } else {
+        // lines fastest: consecutive threads read consecutive l of one position
+        for (int idx = threadIdx.x; idx < NROW * kLines; idx += kThreads) {
+            const int w = idx % kLines, k = idx / kLines;
+            const int j = k / NCH, ch = k % NCH;
+            const long long g = g0 + w;
+            const int p = qc0 + S.lowfil + j;
+            double v = 0.0;
+            if (g < nlines && p <= plast) v = fetch<KIND>(S, x, g, p, ch, in_pext);
+            tile[k * kPad + w] = v;
+        }
+    }
+    __syncthreads();
+
+    const int w = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    const long long g = g0 + w;
+    const long long l = g % S.nL, r = g / S.nL;
+    const double *f = c_ftab + S.ftab;
+    double dot = 0.0;
+    if (g < nlines) {
+        for (int qr = wi; qr < QC; qr += kWarps) {
+            const int q = qc0 + qr;
+            if (q > S.qhi) break;
+            double o0 = 0.0, o1 = 0.0;
+#pragma unroll
+            for (int k = 0; k < NT; ++k) {
+                const int row = (qr + k) * NCH;
+                if (KIND == KCONV) {
+                    o0 = fma(tile[row * kPad + w], f[k], o0);
+                } else if (KIND == KDEC) {          // f = LE | LO | HE | HO
+                    const double x0 = tile[row * kPad + w], x1 = tile[(row + 1) * kPad + w];
+                    o0 = fma(x0, f[k], o0);
+                    o1 = fma(x0, f[2 * NT + k], o1);
+                    o0 = fma(x1, f[NT + k], o0);
+                    o1 = fma(x1, f[3 * NT + k], o1);
+                } else {
+                    const double s = tile[row * kPad + w], d = tile[(row + 1) * kPad + w];
+                    o0 = fma(s, f[NT + k], o0);
+                    o1 = fma(s, f[k], o1);
+                    o0 = fma(d, f[3 * NT + k], o0);
+                    o1 = fma(d, f[2 * NT + k], o1);
+                }
+            }
+#pragma unroll
+            for (int ch = 0; ch < NCH; ++ch) {
+                double out = ch ? o1 : o0;
+                if (S.has_a) out *= S.a;
+                const int pos = q - S.out_lo;
+                const long long off = KIND == KREC ? (long long)ch + 2LL * pos
+                                                   : (long long)pos + (long long)S.out_ext * ch;
+                const long long yi = S.transpose ? r + (long long)S.nR * off
+                                                 : l + (long long)S.nL * (off + out_pext * r);
+                if (KIND == KCONV) {
+                    if ((S.has_dot || S.has_ax) && (S.bc != BC_GROW || (q >= 0 && q < S.n))) {
+                        const double xq = tile[(qr - S.lowfil) * kPad + w];
+                        if (S.has_dot) dot = fma(xq, out, dot);
+                        if (S.has_ax) out = fma(xq, S.a_x, out);
+                    }
+                    if (x2) {
+                        const long long x2i = S.bc == BC_GROW
+                            ? yi : l + (long long)S.nL * ((long long)(q - S.in_lo) + in_pext * r);
+                        out += x2[x2i];
+                    }
+                }
+                if (S.ay_mode == 2) out += y[yi];
+                else if (S.ay_mode == 1) out = fma(S.a_y, y[yi], out);
+                y[yi] = out;
+            }
+        }
+    }
+    if (S.has_dot) {
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+        if (w == 0) red[wi] = dot;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int i = 0; i < kWarps; ++i) s += red[i];
+            const long long b = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+            S.dot_part[b] = s;
+        }
+    }
+}
+
+__global__ void dot_reduce_kernel(const double *__restrict__ part, long long count, double *out,
+                                  int accumulate) {
+    __shared__ double red[256];
+    double s = 0.0;
+    for (long long i = threadIdx.x; i < count; i += blockDim.x) s += part[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = accumulate ? *out + red[0] : red[0];
+}
+
+template <int KIND, int NT>
+cudaError_t launch_t(const Sweep &S, cudaStream_t st) {
+    const long long nlines = (long long)S.nL * S.nR;
+    const int nq = S.qhi - S.qlo + 1;
+    dim3 grid((unsigned)((nlines + kLines - 1) / kLines),
+              (unsigned)((nq + Chunk<KIND>::QC - 1) / Chunk<KIND>::QC), (unsigned)S.narr);
+    sweep_fp64_kernel<KIND, NT><<<grid, kThreads, 0, st>>>(S);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+long long sweep_fp64_blocks(const Sweep &S) {
+    const long long nlines = (long long)S.nL * S.nR;
+    const int qc = S.kind == KCONV ? Chunk<KCONV>::QC : Chunk<KDEC>::QC;
+    const long long nq = S.qhi - S.qlo + 1;
+    return ((nlines + kLines - 1) / kLines) * ((nq + qc - 1) / qc) * S.narr;
+}
+
+cudaError_t launch_sweep_fp64(const Sweep &S, cudaStream_t st) {
+    if (S.kind == KCONV && S.ntaps == 16) return launch_t<KCONV, 16>(S, st);
+    if (S.kind == KCONV && S.ntaps == 29) return launch_t<KCONV, 29>(S, st);
+    if (S.kind == KDEC && S.ntaps == 8) return launch_t<KDEC, 8>(S, st);
+    if (S.kind == KDEC && S.ntaps == 16) return launch_t<KDEC, 16>(S, st);
+    if (S.kind == KREC && S.ntaps == 8) return launch_t<KREC, 8>(S, st);
+    if (S.kind == KREC && S.ntaps == 16) return launch_t<KREC, 16>(S, st);
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_dot_reduce(const double *part, long long count, double *out, int accumulate,
+                              cudaStream_t st) {
+    dot_reduce_kernel<<<1, 256, 0, st>>>(part, count, out, accumulate);
+    return cudaGetLastError();
+}
+
+}  // namespace lcg

@@ -1,0 +1,182 @@
+/* libconv-gb300: GB300 (sm_103a) implementation of BigDFT's separable
+ * Daubechies-16 convolutions (MagicFilter, Kinetic, wavelet analysis and
+ * synthesis) behind the procedure signatures that BOAST generates for them
+ * in Nanosim-LIG/boast-lig (BigDFT/GenericConvolution2.rb).
+ *
+ * Conventions (same as the generated code):
+ *   - arrays are Fortran-ordered (first index fastest), FP64;
+ *   - n[], nx[], ny[], bc[] are small host int arrays of length d;
+ *   - for wavelet operators n/nx/ny count coefficient pairs (the array extent
+ *     along a dimension is twice the value);
+ *   - bc: LIBCONV_BC_PERIODIC (0), LIBCONV_BC_GROW (1), LIBCONV_BC_SHRINK (-1),
+ *     LIBCONV_BC_FREE (2, free boundary without growth);
+ *   - narr independent arrays lie back to back in x and y.
+ *
+ * Every entry point returns LIBCONV_OK (0) or a negative status; the
+ * generated reference procedures return nothing, and a caller that declares
+ * them void may call these functions unchanged.
+ *
+ * Plain entry points take HOST pointers: inputs are copied to the GPU, the
+ * operator runs, the outputs are copied back, and the call returns when the
+ * result is in host memory.  The workspaces w1/w2 of the host-pointer 3D
+ * entry points are accepted for signature compatibility and left untouched.
+ * The *_dev entry points take DEVICE pointers and a cudaStream_t (passed as
+ * void*, NULL = legacy default stream); they only enqueue work, and a
+ * dot_in output of a *_dev entry point is a device pointer.
+ */
+#ifndef LIBCONV_GB300_H
+#define LIBCONV_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LIBCONV_OK        0
+#define LIBCONV_EARG     -1   /* bad argument (null pointer, d/idim/n/narr out of range) */
+#define LIBCONV_EBC      -2   /* boundary condition not supported by this operator */
+#define LIBCONV_ESIZE    -3   /* nx/ny leading sizes too small for n and bc */
+#define LIBCONV_ECUDA    -4   /* CUDA runtime error (message in libconv_gb300_last_error) */
+#define LIBCONV_ENOMEM   -5   /* device allocation failed */
+#define LIBCONV_EMODE    -6   /* unknown compute mode */
+
+#define LIBCONV_BC_SHRINK   -1
+#define LIBCONV_BC_PERIODIC  0
+#define LIBCONV_BC_GROW      1
+#define LIBCONV_BC_FREE      2
+
+/* Compute modes for libconv_gb300_set_mode (per calling thread).
+ *   FP64: plain FP64 FMA kernels on the CUDA cores (default). */
+#define LIBCONV_MODE_FP64   0
+
+const char *libconv_gb300_version(void);
+const char *libconv_gb300_strerror(int status);
+/* Detailed message of the last failing call on this thread ("" if none). */
+const char *libconv_gb300_last_error(void);
+int libconv_gb300_set_mode(int mode);
+int libconv_gb300_get_mode(void);
+
+/* ---------------------------------------------------------------------
+ * 1D sweeps: GenericConvolutionOperator1d#procedure
+ * (BigDFT/GenericConvolution2.rb:1560-1764), the ld + narr variants that
+ * MagicFilter1d/Kinetic1d/Wavelet1d generate.  Shapes [1,0] / [0,1] /
+ * [2,0,1] are selected from idim as the reference does (:1701-1761).
+ *   y = a * fil (x)_idim x + a_x * x + a_y * y
+ * ------------------------------------------------------------------- */
+
+/* MagicFilter, filter 'sym8_md' = reverse(SYM8_MF), lowfil -8
+ * (BigDFT/LibconvBase.rb:238-242; BigDFT/MagicFilter1d2.rb:5-24). */
+int d_s0s0_1d_sym8_md(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                      int narr, const double *x, double *y, double a, double a_x, double a_y);
+/* Inverse MagicFilter, filter 'sym8_imd' = SYM8_MF, lowfil -7
+ * (BigDFT/LibconvBase.rb:244-248). */
+int d_s0s0_1d_sym8_imd(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                       int narr, const double *x, double *y, double a, double a_x, double a_y);
+/* First-derivative filter SYM8_D1 (29 taps) through the same generic
+ * operator (BigDFT/WaveletFilters.rb:43-72; libconv.f90:412-413). */
+int d_s0s0_1d_sym8_d1(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                      int narr, const double *x, double *y, double a, double a_x, double a_y);
+/* Kinetic second derivative SYM8_D2 (29 taps) with the energy term
+ * dot_in = sum x * (a * D2 x), taken before a_x is added
+ * (BigDFT/Kinetic1d.rb:6-25; GenericConvolution2.rb:179-181).
+ * dot_in sums over all narr arrays. */
+int d_s0s0_1d_sym8_d2_dotin(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                            int narr, const double *x, double *y, double a, double a_x,
+                            double a_y, double *dot_in);
+/* Wavelet analysis (dwt), WaveletFilterDecompose of SYM8_LP:
+ * x(0:1, p) interleaved -> y(q, 0:1) low block then high block
+ * (BigDFT/LibconvBase.rb:226-230; GenericConvolution2.rb:505-587). */
+int d_s0s1_1d_sym8(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                   int narr, const double *x, double *y, double a, double a_y);
+/* Wavelet synthesis (idwt), WaveletFilterRecompose of SYM8_LP
+ * (BigDFT/LibconvBase.rb:232-236; GenericConvolution2.rb:589-671). */
+int d_s1s0_1d_sym8(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                   int narr, const double *x, double *y, double a, double a_y);
+/* s1tor: synthesis fused with the MagicFilter (combined filters of
+ * GenericConvolution2.rb:336-384; BigDFT/LibconvBase.rb:250-255). */
+int d_s1s0_1d_symicomb8(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                        int narr, const double *x, double *y, double a, double a_y);
+/* rtos1: analysis fused with the MagicFilter (BigDFT/LibconvBase.rb:257-262). */
+int d_s0s1_1d_symicomb8(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                        int narr, const double *x, double *y, double a, double a_y);
+
+int d_s0s0_1d_sym8_md_dev(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                          int narr, const double *x, double *y, double a, double a_x, double a_y,
+                          void *stream);
+int d_s0s0_1d_sym8_imd_dev(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                           int narr, const double *x, double *y, double a, double a_x,
+                           double a_y, void *stream);
+int d_s0s0_1d_sym8_d1_dev(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                          int narr, const double *x, double *y, double a, double a_x, double a_y,
+                          void *stream);
+int d_s0s0_1d_sym8_d2_dotin_dev(int d, int idim, const int *n, int bc, const int *nx,
+                                const int *ny, int narr, const double *x, double *y, double a,
+                                double a_x, double a_y, double *dot_in, void *stream);
+int d_s0s1_1d_sym8_dev(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                       int narr, const double *x, double *y, double a, double a_y, void *stream);
+int d_s1s0_1d_sym8_dev(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                       int narr, const double *x, double *y, double a, double a_y, void *stream);
+int d_s1s0_1d_symicomb8_dev(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                            int narr, const double *x, double *y, double a, double a_y,
+                            void *stream);
+int d_s0s1_1d_symicomb8_dev(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                            int narr, const double *x, double *y, double a, double a_y,
+                            void *stream);
+
+/* ---------------------------------------------------------------------
+ * Multi-dimensional operators: GenericConvolutionOperator#procedure
+ * (BigDFT/GenericConvolution2.rb:1934-2243).
+ * ------------------------------------------------------------------- */
+
+/* 3D MagicFilter (transpose = 1, ld, narr, work): MagicFilter() of
+ * BigDFT/MagicFilter2.rb:46-70 built on the filter named 'sfrf' in
+ * BigDFT/MagicFilter_test2.rb:60 (reverse(SYM8_MF) centre 8). */
+int d_sfrf_ld_narr(int d, const int *n, const int *bc, const int *nx, const int *ny, int narr,
+                   const double *x, double *y, double *w1, double *w2);
+/* Same with the inverse filter 'rfsf' (BigDFT/MagicFilter_test2.rb:152). */
+int d_rfsf_ld_narr(int d, const int *n, const int *bc, const int *nx, const int *ny, int narr,
+                   const double *x, double *y, double *w1, double *w2);
+/* 3D kinetic (transpose = 0, a[d], a_x, a_y, kinetic, zero_out_work):
+ * Kinetic() of BigDFT/Kinetic2.rb:1068-1090 on the filter 'kin'
+ * (BigDFT/Kinetic_test2.rb:33):  y = sum_i a[i] D2_i x + a_x x + a_y y.
+ * Periodic and free (no-grow) boundaries. */
+int d_kin(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
+          double *w2, const double *a, double a_x, double a_y);
+/* 3D wavelet analysis / synthesis (transpose = 1, work): Wavelet() of
+ * BigDFT/Wavelet2.rb:2-21 (BigDFT/Wavelet_test2.rb:86-154). */
+int d_dwt_sym8(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
+               double *w2);
+int d_idwt_sym8(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
+                double *w2);
+
+/* Device-pointer forms; w1/w2 are device workspaces sized like the
+ * reference's (the largest intermediate grid, times narr). */
+int d_sfrf_ld_narr_dev(int d, const int *n, const int *bc, const int *nx, const int *ny,
+                       int narr, const double *x, double *y, double *w1, double *w2,
+                       void *stream);
+int d_rfsf_ld_narr_dev(int d, const int *n, const int *bc, const int *nx, const int *ny,
+                       int narr, const double *x, double *y, double *w1, double *w2,
+                       void *stream);
+int d_kin_dev(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
+              double *w2, const double *a, double a_x, double a_y, void *stream);
+int d_dwt_sym8_dev(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
+                   double *w2, void *stream);
+int d_idwt_sym8_dev(int d, const int *n, const int *bc, const double *x, double *y,
+                    double *w1, double *w2, void *stream);
+
+/* ---------------------------------------------------------------------
+ * Cost model (ConvolutionOperator1d#cost / GenericConvolutionOperator#cost,
+ * BigDFT/GenericConvolution2.rb:1269-1276, 1850-1932): the flop count the
+ * reference uses for every GFlop/s it prints (n * filter.cost * ndat per
+ * sweep; filter.cost = 2*taps for convolutions, 4*length for wavelets).
+ * ------------------------------------------------------------------- */
+int d_s0s0_1d_sym8_md_cost(int d, int idim, const int *n, int bc, int narr, long long *cost);
+int d_s0s0_1d_sym8_d2_cost(int d, int idim, const int *n, int bc, int narr, long long *cost);
+int d_s0s1_1d_sym8_cost(int d, int idim, const int *n, int bc, int narr, long long *cost);
+int d_sfrf_cost(int d, const int *n, const int *bc, int narr, long long *cost);
+int d_kin_cost(int d, const int *n, const int *bc, long long *cost);
+int d_dwt_sym8_cost(int d, const int *n, const int *bc, long long *cost);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LIBCONV_GB300_H */

@@ -1,0 +1,509 @@
+/* CPU oracle for libconv-gb300 -- TEST INFRASTRUCTURE ONLY (see libconv_oracle.h).
+ *
+ * Plain C99, FP64, single-threaded, compiled with -ffp-contract=off so that
+ * the x86 and aarch64 builds give the same bits.  Tap order and
+ * post-processing order follow the reference line by line (citations inline).
+ */
+#include <stddef.h>
+#include <stdint.h>
+#include "libconv_oracle.h"
+#include "../boast-lig_gb300/csrc/libconv_filters.h"
+
+/* Boundary-condition ids: GenericConvolution2.rb:684-689. */
+enum { BC_SHRINK = -1, BC_PERIODIC = 0, BC_GROW = 1, BC_FREE = 2 };
+/* Error codes shared with the GPU library (include/libconv_gb300.h). */
+enum { OK = 0, E_ARG = -1, E_BC = -2, E_SIZE = -3 };
+enum { K_CONV = 0, K_DEC = 1, K_REC = 2 };
+
+static int imod(int a, int n) { int r = a % n; return r < 0 ? r + n : r; }
+
+/* ======================================================================
+ * Fortran reference kernels
+ * ====================================================================== */
+
+/* BigDFT/magicfilter_refs.f90:92-133.  x(0:n1-1,ndat) -> y(ndat,0:n1-1). */
+void oracle_magicfilter_per_ref(int n1, int ndat, const double *x, double *y)
+{
+    for (int j = 0; j < ndat; ++j)
+        for (int i = 0; i < n1; ++i) {
+            double tt = 0.0;
+            for (int l = -8; l <= 7; ++l)
+                tt = tt + x[imod(i + l, n1) + (size_t)n1 * j] * LCG_MF_FORTRAN[l + 8];
+            y[j + (size_t)ndat * i] = tt;
+        }
+}
+
+/* BigDFT/magicfilter_refs.f90:135-181: reversed filter, lowfil=-7. */
+void oracle_magicfilter_per_t_ref(int n1, int ndat, const double *x, double *y)
+{
+    for (int j = 0; j < ndat; ++j)
+        for (int i = 0; i < n1; ++i) {
+            double tt = 0.0;
+            for (int l = -7; l <= 8; ++l)
+                tt = tt + x[imod(i + l, n1) + (size_t)n1 * j] * LCG_MF_FORTRAN[15 - (l + 7)];
+            y[j + (size_t)ndat * i] = tt;
+        }
+}
+
+/* BigDFT/magicfilter_refs.f90:2-44: grow, y(ndat,-7:n1+7), clipped taps. */
+void oracle_magicfilter_free_ref(int n1, int ndat, const double *x, double *y)
+{
+    for (int j = 0; j < ndat; ++j)
+        for (int i = -7; i <= n1 - 1 + 8; ++i) {
+            double tt = 0.0;
+            int lo = -i > -8 ? -i : -8, hi = 7 < n1 - 1 - i ? 7 : n1 - 1 - i;
+            for (int l = lo; l <= hi; ++l)
+                tt = tt + x[(i + l) + (size_t)n1 * j] * LCG_MF_FORTRAN[l + 8];
+            y[j + (size_t)ndat * (i + 7)] = tt;
+        }
+}
+
+/* BigDFT/magicfilter_refs.f90:48-90: shrink, x(-7:n1+7,ndat) -> y(ndat,0:n1-1). */
+void oracle_magicfilter_free_t_ref(int n1, int ndat, const double *x, double *y)
+{
+    const int ext = n1 + 15;
+    for (int j = 0; j < ndat; ++j)
+        for (int i = 0; i < n1; ++i) {
+            double tt = 0.0;
+            for (int l = -7; l <= 8; ++l)
+                tt = tt + x[(i + l + 7) + (size_t)ext * j] * LCG_MF_FORTRAN[15 - (l + 7)];
+            y[j + (size_t)ndat * i] = tt;
+        }
+}
+
+/* BigDFT/Kinetic2.rb:981-1061 (kinetic_per_ref): y = c*x + sum_d scale_d*D2_d x,
+ * scale_d = -0.5/h_d^2 folded into the filter as the Fortran does. */
+void oracle_kinetic_per_ref(int n1, int n2, int n3, const double *hgrid,
+                            const double *x, double *y, double c)
+{
+    double fil[3][29];
+    for (int d = 0; d < 3; ++d) {
+        double scale = -0.5 / (hgrid[d] * hgrid[d]);
+        for (int i = 0; i <= 14; ++i) {
+            fil[d][14 + i] = LCG_KIN_FORTRAN[i] * scale;
+            fil[d][14 - i] = fil[d][14 + i];
+        }
+    }
+#define X(a, b, c_) x[(a) + (size_t)n1 * ((b) + (size_t)n2 * (c_))]
+#define Y(a, b, c_) y[(a) + (size_t)n1 * ((b) + (size_t)n2 * (c_))]
+    for (int i3 = 0; i3 < n3; ++i3) {
+        for (int i2 = 0; i2 < n2; ++i2)
+            for (int i1 = 0; i1 < n1; ++i1) {
+                double tt = X(i1, i2, i3) * c;
+                for (int l = -14; l <= 14; ++l)
+                    tt = tt + X(imod(i1 + l, n1), i2, i3) * fil[0][l + 14];
+                Y(i1, i2, i3) = tt;
+            }
+        for (int i1 = 0; i1 < n1; ++i1)
+            for (int i2 = 0; i2 < n2; ++i2) {
+                double tt = 0.0;
+                for (int l = -14; l <= 14; ++l)
+                    tt = tt + X(i1, imod(i2 + l, n2), i3) * fil[1][l + 14];
+                Y(i1, i2, i3) = Y(i1, i2, i3) + tt;
+            }
+    }
+    for (int i2 = 0; i2 < n2; ++i2)
+        for (int i1 = 0; i1 < n1; ++i1)
+            for (int i3 = 0; i3 < n3; ++i3) {
+                double tt = 0.0;
+                for (int l = -14; l <= 14; ++l)
+                    tt = tt + X(i1, i2, imod(i3 + l, n3)) * fil[2][l + 14];
+                Y(i1, i2, i3) = Y(i1, i2, i3) + tt;
+            }
+#undef X
+#undef Y
+}
+
+/* ch(-8:9), cg(-8:9) of old/Synthesis.rb:32-47: the 16 Daubechies taps
+ * padded with one zero on each side. */
+static double ch_s(int m) { return (m < -7 || m > 8) ? 0.0 : LCG_CH_FORTRAN[m + 7]; }
+static double cg_s(int m) { return (m < -7 || m > 8) ? 0.0 : LCG_CG_FORTRAN[m + 7]; }
+
+/* old/Synthesis.rb:100-146: x(0:2n-1,ndat) [s|d] -> y(ndat,0:2n-1) interleaved. */
+void oracle_synthesis_per_ref(int n, int ndat, const double *x, double *y)
+{
+    for (int j = 0; j < ndat; ++j) {
+        const double *xj = x + (size_t)2 * n * j;
+        for (int i = 0; i < n; ++i) {
+            double se = 0.0, so = 0.0;
+            for (int l = -4; l <= 4; ++l) {
+                int k = imod(i - l, n);
+                se = se + ch_s(2 * l) * xj[k] + cg_s(2 * l) * xj[n + k];
+                so = so + ch_s(2 * l + 1) * xj[k] + cg_s(2 * l + 1) * xj[n + k];
+            }
+            y[j + (size_t)ndat * (2 * i)] = se;
+            y[j + (size_t)ndat * (2 * i + 1)] = so;
+        }
+    }
+}
+
+/* old/Synthesis.rb:23-82: free (grow), y(ndat,-7:2n+6). */
+void oracle_synthesis_free_ref(int n, int ndat, const double *x, double *y)
+{
+#define YF(jj, m) y[(jj) + (size_t)ndat * ((m) + 7)]
+    for (int j = 0; j < ndat; ++j) {
+        const double *xj = x + (size_t)2 * n * j;
+        int i = -4;
+        double so = 0.0, se;
+        for (int l = (i - n + 1 > -4 ? i - n + 1 : -4); l <= (i < 4 ? i : 4); ++l)
+            so = so + ch_s(2 * l + 1) * xj[i - l] + cg_s(2 * l + 1) * xj[n + i - l];
+        YF(j, 2 * i + 1) = so;
+        for (i = -3; i <= n + 2; ++i) {
+            se = 0.0; so = 0.0;
+            for (int l = (i - n + 1 > -4 ? i - n + 1 : -4); l <= (i < 4 ? i : 4); ++l) {
+                se = se + ch_s(2 * l) * xj[i - l] + cg_s(2 * l) * xj[n + i - l];
+                so = so + ch_s(2 * l + 1) * xj[i - l] + cg_s(2 * l + 1) * xj[n + i - l];
+            }
+            YF(j, 2 * i) = se;
+            YF(j, 2 * i + 1) = so;
+        }
+        i = n + 3;
+        se = 0.0;
+        for (int l = (i - n + 1 > -4 ? i - n + 1 : -4); l <= (i < 4 ? i : 4); ++l)
+            se = se + ch_s(2 * l) * xj[i - l] + cg_s(2 * l) * xj[n + i - l];
+        YF(j, 2 * i) = se;
+    }
+#undef YF
+}
+
+/* Periodic analysis.  The live reference (old/AnaRotPer-2.rb:86-221) is an
+ * unrolled form sized 0:2n+1 with a modulo table; its plain form is kept in
+ * the same file (:258-296): ci = sum_{l=-7..8} ch(l) x(mod(l+2i,2n)). */
+void oracle_analysis_per_ref(int n, int ndat, const double *x, double *y)
+{
+    for (int j = 0; j < ndat; ++j) {
+        const double *xj = x + (size_t)2 * n * j;
+        for (int i = 0; i < n; ++i) {
+            double ci = 0.0, di = 0.0;
+            for (int l = -7; l <= 8; ++l) {
+                int k = imod(l + 2 * i, 2 * n);
+                ci = ci + LCG_CH_FORTRAN[l + 7] * xj[k];
+                di = di + LCG_CG_FORTRAN[l + 7] * xj[k];
+            }
+            y[j + (size_t)ndat * i] = ci;
+            y[j + (size_t)ndat * (n + i)] = di;
+        }
+    }
+}
+
+/* old/AnaRotPer-2.rb:22-64: free (shrink), x(-7:2n+6,ndat) -> y(ndat,0:2n-1). */
+void oracle_analysis_free_ref(int n, int ndat, const double *x, double *y)
+{
+    for (int j = 0; j < ndat; ++j) {
+        const double *xj = x + (size_t)(2 * n + 14) * j;
+        for (int i = 0; i < n; ++i) {
+            double ci = 0.0, di = 0.0;
+            for (int l = -7; l <= 8; ++l) {
+                ci = ci + LCG_CH_FORTRAN[l + 7] * xj[l + 2 * i + 7];
+                di = di + LCG_CG_FORTRAN[l + 7] * xj[l + 2 * i + 7];
+            }
+            y[j + (size_t)ndat * i] = ci;
+            y[j + (size_t)ndat * (n + i)] = di;
+        }
+    }
+}
+
+/* ======================================================================
+ * Generated 1D operator (ConvolutionOperator1d, GenericConvolution2.rb)
+ * ====================================================================== */
+
+typedef struct {
+    int kind;       /* K_CONV, K_DEC (s0s1) or K_REC (s1s0) */
+    int lowfil;     /* first tap (polyphase taps for wavelets) */
+    int ntaps;
+    int length;     /* filter.length: taps (conv) or full low-pass length (wavelets) */
+    const double *f;                    /* conv taps, index l - lowfil */
+    const double *le, *lo, *he, *ho;    /* wavelet polyphase filters */
+} ofilt;
+
+typedef struct {
+    int nL, n, nR;          /* ndat_left, processed size (pairs for wavelets), ndat_right */
+    int ld, nx, ny;         /* processed-dim leading sizes (pairs for wavelets) */
+    int transpose;          /* 1: output index rotated (only with nL == 1) */
+    const double *x, *x2;
+    double *y;
+    int has_a;  double a;
+    int has_ax; double a_x;
+    int ay_mode; double a_y;  /* 0: y written, 1: y = a_y*y + out, 2: y = y + out */
+    double *dot;              /* accumulated when non-NULL */
+} ocall;
+
+static int upfil_of(const ofilt *F) { return F->lowfil + F->ntaps - 1; }
+
+/* Input bounds of the processed dim (GenericConvolution2.rb:61-72, 206-223). */
+static void in_bounds(const ofilt *F, int bc, const ocall *c, int *lo, int *ext)
+{
+    if (bc == BC_SHRINK) { *lo = F->lowfil; *ext = c->ld ? c->nx : c->n + upfil_of(F) - F->lowfil; }
+    else { *lo = 0; *ext = c->ld ? c->nx : c->n; }
+}
+/* Output bounds (GenericConvolution2.rb:74-85, 215-225). */
+static void out_bounds(const ofilt *F, int bc, const ocall *c, int *lo, int *ext)
+{
+    if (bc == BC_GROW) { *lo = -upfil_of(F); *ext = c->ld ? c->ny : c->n + upfil_of(F) - F->lowfil; }
+    else { *lo = 0; *ext = c->ld ? c->ny : c->n; }
+}
+
+/* Offset of (position pos, channel ch) inside one line of the processed dim. */
+static size_t proc_off(int layout_interleaved, int pos, int ch, int ext)
+{
+    return layout_interleaved ? (size_t)ch + 2 * (size_t)pos : (size_t)pos + (size_t)ext * ch;
+}
+
+static void conv1d(const ofilt *F, int bc, const ocall *c)
+{
+    const int wav = F->kind != K_CONV;
+    const int nch = wav ? 2 : 1;
+    int ilo, iext, olo, oext;
+    in_bounds(F, bc, c, &ilo, &iext);
+    out_bounds(F, bc, c, &olo, &oext);
+    const size_t ipext = (size_t)iext * nch, opext = (size_t)oext * nch;
+    const int in_il = F->kind == K_DEC;   /* decompose input interleaved x(0:1, p) */
+    const int out_il = F->kind == K_REC;  /* recompose output interleaved y(0:1, q) */
+    const int up = upfil_of(F);
+    const int qlo = bc == BC_GROW ? -up : 0;
+    const int qhi = bc == BC_GROW ? c->n - F->lowfil - 1 : c->n - 1;
+    const int clip = (bc == BC_GROW || bc == BC_FREE);
+
+    for (int r = 0; r < c->nR; ++r)
+        for (int l = 0; l < c->nL; ++l) {
+#define XIN(pos, ch) c->x[(size_t)l + (size_t)c->nL * (proc_off(in_il, (pos), (ch), iext) + ipext * r)]
+            for (int q = qlo; q <= qhi; ++q) {
+                int lmin = F->lowfil, lmax = up;
+                if (clip) {   /* GenericConvolution2.rb:91-104, clipped on both sides */
+                    if (lmin < -q) lmin = -q;
+                    if (lmax > c->n - 1 - q) lmax = c->n - 1 - q;
+                }
+                double o0 = 0.0, o1 = 0.0;
+                for (int t = lmin; t <= lmax; ++t) {
+                    int p = q + t;
+                    if (bc == BC_PERIODIC) p = imod(p, c->n);
+                    int pos = p - ilo;
+                    int k = t - F->lowfil;
+                    if (F->kind == K_CONV) {
+                        o0 = o0 + XIN(pos, 0) * F->f[k];                /* :168-171 */
+                    } else if (F->kind == K_DEC) {                      /* :453-462, 471-476 */
+                        double x0 = XIN(pos, 0), x1 = XIN(pos, 1);
+                        o0 = o0 + x0 * F->le[k];
+                        o1 = o1 + x0 * F->he[k];
+                        o0 = o0 + x1 * F->lo[k];
+                        o1 = o1 + x1 * F->ho[k];
+                    } else {                                            /* :453-462, 600-605 */
+                        double s = XIN(pos, 0), dd = XIN(pos, 1);
+                        o0 = o0 + s * F->lo[k];
+                        o1 = o1 + s * F->le[k];
+                        o0 = o0 + dd * F->ho[k];
+                        o1 = o1 + dd * F->he[k];
+                    }
+                }
+                double outv[2] = { o0, o1 };
+                for (int ch = 0; ch < nch; ++ch) {
+                    double out = outv[ch];
+                    if (c->has_a) out = out * c->a;                     /* :177 / :469-472 */
+                    size_t oo = proc_off(out_il, q - olo, ch, oext);
+                    size_t yi = c->transpose ? (size_t)r + (size_t)c->nR * oo
+                                             : (size_t)l + (size_t)c->nL * (oo + opext * r);
+                    if (!wav) {
+                        /* :179-190: dot_in before a_x; grow only inside the input */
+                        if ((c->dot || c->has_ax) && (bc != BC_GROW || (q >= 0 && q < c->n))) {
+                            double xq = XIN(q - ilo, 0);
+                            if (c->dot) *c->dot = *c->dot + xq * out;
+                            if (c->has_ax) out = xq * c->a_x + out;
+                        }
+                        if (c->x2) {                                    /* :193 */
+                            size_t x2i = bc == BC_GROW ? yi
+                                : (size_t)l + (size_t)c->nL * ((size_t)(q - ilo) + ipext * r);
+                            out = out + c->x2[x2i];
+                        }
+                    }
+                    if (c->ay_mode == 2) out = out + c->y[yi];          /* :195-199 */
+                    else if (c->ay_mode == 1) out = c->a_y * c->y[yi] + out;
+                    c->y[yi] = out;
+                }
+            }
+#undef XIN
+        }
+}
+
+/* ---- filter objects ---- */
+static const ofilt F_MD = { K_CONV, LCG_CONV_SYM8_MD_LOWFIL, 16, 16, LCG_CONV_SYM8_MD, 0, 0, 0, 0 };
+static const ofilt F_IMD = { K_CONV, LCG_CONV_SYM8_IMD_LOWFIL, 16, 16, LCG_CONV_SYM8_IMD, 0, 0, 0, 0 };
+static const ofilt F_D2 = { K_CONV, LCG_CONV_SYM8_D2_LOWFIL, 29, 29, LCG_SYM8_D2, 0, 0, 0, 0 };
+static const ofilt F_D1 = { K_CONV, LCG_CONV_SYM8_D1_LOWFIL, 29, 29, LCG_SYM8_D1, 0, 0, 0, 0 };
+#define WT(TAG, KIND) { KIND, TAG##_LOWFIL, TAG##_NTAPS, TAG##_LENGTH, 0, TAG##_LE, TAG##_LO, TAG##_HE, TAG##_HO }
+static const ofilt F_DWT_P = WT(LCG_WT_SYM8_DEC_P, K_DEC);
+static const ofilt F_DWT_GS = WT(LCG_WT_SYM8_DEC_GS, K_DEC);
+static const ofilt F_IWT_P = WT(LCG_WT_SYM8_REC_P, K_REC);
+static const ofilt F_IWT_GS = WT(LCG_WT_SYM8_REC_GS, K_REC);
+static const ofilt F_RTOS1_P = WT(LCG_WT_SYMICOMB8_DEC_P, K_DEC);
+static const ofilt F_RTOS1_GS = WT(LCG_WT_SYMICOMB8_DEC_GS, K_DEC);
+static const ofilt F_S1TOR_P = WT(LCG_WT_SYMICOMB8_REC_P, K_REC);
+static const ofilt F_S1TOR_GS = WT(LCG_WT_SYMICOMB8_REC_GS, K_REC);
+
+static int bc_ok(int bc) { return bc == BC_PERIODIC || bc == BC_GROW || bc == BC_SHRINK || bc == BC_FREE; }
+
+/* Required extents of the processed dim (pairs for wavelets). */
+static int need_in(const ofilt *F, int bc, int n) { return bc == BC_SHRINK ? n + F->ntaps - 1 : n; }
+static int need_out(const ofilt *F, int bc, int n) { return bc == BC_GROW ? n + F->ntaps - 1 : n; }
+
+/* ======================================================================
+ * 1D dispatcher: GenericConvolutionOperator1d#procedure, GenericConvolution2.rb:1560-1764
+ * d_<base>_1d_<fil>(d, idim, n[], bc, nx[], ny[], narr, x, y, a, [a_x,] a_y [, dot_in])
+ * ====================================================================== */
+static int disp1d(const ofilt *Fp, const ofilt *Fgs, int d, int idim, const int *n, int bc,
+                  const int *nx, const int *ny, int narr, const double *x, double *y,
+                  double a, int use_ax, double a_x, double a_y, double *dot_in)
+{
+    if (d < 1 || idim < 0 || idim >= d || narr < 1 || !n || !nx || !ny || !x || !y) return E_ARG;
+    if (!bc_ok(bc)) return E_BC;
+    const ofilt *F = (bc == BC_GROW || bc == BC_SHRINK) ? Fgs : Fp;
+    const int mul = F->kind == K_CONV ? 1 : 2;
+    for (int i = 0; i < d; ++i) if (n[i] < 1 || nx[i] < 1 || ny[i] < 1) return E_ARG;
+    if (nx[idim] < need_in(F, bc, n[idim]) || ny[idim] < need_out(F, bc, n[idim])) return E_SIZE;
+    long nL = 1, nR = 1;
+    for (int i = 0; i < idim; ++i) nL *= (long)nx[i] * mul;       /* :1725-1733 */
+    for (int i = idim + 1; i < d; ++i) nR *= (long)nx[i] * mul;
+    size_t nti = (size_t)nx[idim] * mul * nL * nR, nto = (size_t)ny[idim] * mul * nL * nR;
+    ocall c = { (int)nL, n[idim], (int)nR, 1, nx[idim], ny[idim], 0, 0, 0, 0,
+                a != 1.0, a, use_ax && a_x != 0.0, a_x, a_y != 0.0 ? 1 : 0, a_y, 0 };
+    double acc = 0.0;
+    if (dot_in) c.dot = &acc;
+    for (int j = 0; j < narr; ++j) {                                  /* :1611-1618 */
+        c.x = x + nti * j;
+        c.y = y + nto * j;
+        conv1d(F, bc, &c);
+    }
+    if (dot_in) *dot_in = acc;   /* sum over the narr arrays */
+    return OK;
+}
+
+int oracle_d_s0s0_1d_sym8_md(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                             int narr, const double *x, double *y, double a, double a_x, double a_y)
+{ return disp1d(&F_MD, &F_MD, d, idim, n, bc, nx, ny, narr, x, y, a, 1, a_x, a_y, 0); }
+int oracle_d_s0s0_1d_sym8_imd(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                              int narr, const double *x, double *y, double a, double a_x, double a_y)
+{ return disp1d(&F_IMD, &F_IMD, d, idim, n, bc, nx, ny, narr, x, y, a, 1, a_x, a_y, 0); }
+int oracle_d_s0s0_1d_sym8_d1(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                             int narr, const double *x, double *y, double a, double a_x, double a_y)
+{ return disp1d(&F_D1, &F_D1, d, idim, n, bc, nx, ny, narr, x, y, a, 1, a_x, a_y, 0); }
+int oracle_d_s0s0_1d_sym8_d2_dotin(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                                   int narr, const double *x, double *y, double a, double a_x,
+                                   double a_y, double *dot_in)
+{
+    double dummy;
+    return disp1d(&F_D2, &F_D2, d, idim, n, bc, nx, ny, narr, x, y, a, 1, a_x, a_y,
+                  dot_in ? dot_in : &dummy);
+}
+int oracle_d_s0s1_1d_sym8(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                          int narr, const double *x, double *y, double a, double a_y)
+{ return disp1d(&F_DWT_P, &F_DWT_GS, d, idim, n, bc, nx, ny, narr, x, y, a, 0, 0.0, a_y, 0); }
+int oracle_d_s1s0_1d_sym8(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                          int narr, const double *x, double *y, double a, double a_y)
+{ return disp1d(&F_IWT_P, &F_IWT_GS, d, idim, n, bc, nx, ny, narr, x, y, a, 0, 0.0, a_y, 0); }
+int oracle_d_s0s1_1d_symicomb8(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                               int narr, const double *x, double *y, double a, double a_y)
+{ return disp1d(&F_RTOS1_P, &F_RTOS1_GS, d, idim, n, bc, nx, ny, narr, x, y, a, 0, 0.0, a_y, 0); }
+int oracle_d_s1s0_1d_symicomb8(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                               int narr, const double *x, double *y, double a, double a_y)
+{ return disp1d(&F_S1TOR_P, &F_S1TOR_GS, d, idim, n, bc, nx, ny, narr, x, y, a, 0, 0.0, a_y, 0); }
+
+/* ======================================================================
+ * Multi-D transposed dispatcher (transpose = 1): GenericConvolution2.rb:1934-2243
+ * used by MagicFilter() (ld, narr, work) and Wavelet() (work).
+ * Each sweep is shape [1,0] with the output index rotated, so after d
+ * sweeps the array is back in its original orientation.
+ * ====================================================================== */
+static int dispmd_t(const ofilt *Fp, const ofilt *Fgs, int d, const int *n, const int *bc,
+                    const int *nx, const int *ny, int narr, const double *x, double *y,
+                    double *w1, double *w2)
+{
+    if (d < 1 || d > 16 || narr < 1 || !n || !bc || !x || !y) return E_ARG;
+    if (d > 1 && (!w1 || (d > 2 && !w2))) return E_ARG;
+    const int ld = nx != 0;
+    if (ld && !ny) return E_ARG;
+    long dims[16];
+    const int mul = Fp->kind == K_CONV ? 1 : 2;
+    for (int i = 0; i < d; ++i) {
+        if (n[i] < 1) return E_ARG;
+        if (!bc_ok(bc[i])) return E_BC;
+        const ofilt *F = (bc[i] == BC_GROW || bc[i] == BC_SHRINK) ? Fgs : Fp;
+        if (ld) {
+            if (nx[i] < need_in(F, bc[i], n[i]) || ny[i] < need_out(F, bc[i], n[i])) return E_SIZE;
+            dims[i] = (long)nx[i] * mul;                                 /* :1966-1972 */
+        } else {
+            dims[i] = (long)need_in(F, bc[i], n[i]) * mul;                /* :1973-1984 */
+        }
+    }
+    for (int i = 0; i < d; ++i) {
+        const ofilt *F = (bc[i] == BC_GROW || bc[i] == BC_SHRINK) ? Fgs : Fp;
+        long ndat = 1;
+        for (int j = 0; j < d; ++j) if (j != i) ndat *= dims[j];
+        const double *src;
+        double *dst;
+        if (d == 1) { src = x; dst = y; }
+        else if (i == 0) { src = x; dst = w1; }
+        else if (i == d - 1) { src = ((d - 1) % 2 == 1) ? w1 : w2; dst = y; }
+        else { src = (i % 2 == 1) ? w1 : w2; dst = (i % 2 == 1) ? w2 : w1; }
+        /* ping-pong of :2155-2240: w1->w2 on odd sweeps, w2->w1 on even ones,
+         * the last sweep writes y */
+        long out_ext = ld ? (long)ny[i] * mul : (long)need_out(F, bc[i], n[i]) * mul;
+        ocall c = { 1, n[i], (int)ndat, ld, ld ? nx[i] : 0, ld ? ny[i] : 0, 1, 0, 0, 0,
+                    0, 1.0, 0, 0.0, 0, 0.0, 0 };
+        size_t nti = (size_t)ndat * dims[i], nto = (size_t)ndat * out_ext;
+        for (int j = 0; j < narr; ++j) {
+            c.x = src + nti * j;
+            c.y = dst + nto * j;
+            conv1d(F, bc[i], &c);
+        }
+        dims[i] = out_ext;
+    }
+    return OK;
+}
+
+int oracle_d_sfrf_ld_narr(int d, const int *n, const int *bc, const int *nx, const int *ny,
+                          int narr, const double *x, double *y, double *w1, double *w2)
+{ return dispmd_t(&F_MD, &F_MD, d, n, bc, nx, ny, narr, x, y, w1, w2); }
+int oracle_d_rfsf_ld_narr(int d, const int *n, const int *bc, const int *nx, const int *ny,
+                          int narr, const double *x, double *y, double *w1, double *w2)
+{ return dispmd_t(&F_IMD, &F_IMD, d, n, bc, nx, ny, narr, x, y, w1, w2); }
+int oracle_d_dwt_sym8(int d, const int *n, const int *bc, const double *x, double *y,
+                      double *w1, double *w2)
+{ return dispmd_t(&F_DWT_P, &F_DWT_GS, d, n, bc, 0, 0, 1, x, y, w1, w2); }
+int oracle_d_idwt_sym8(int d, const int *n, const int *bc, const double *x, double *y,
+                       double *w1, double *w2)
+{ return dispmd_t(&F_IWT_P, &F_IWT_GS, d, n, bc, 0, 0, 1, x, y, w1, w2); }
+
+/* ======================================================================
+ * Multi-D kinetic dispatcher (transpose = 0, kinetic, zero_out_work):
+ * Kinetic2.rb:1068-1090 with GenericConvolution2.rb:2155-2240.
+ *   sweep 0 (shape [1,0]):     w1 = a[0] D x + a_x x
+ *   middle  (shape [2,0,1]):   w' = a[i] D_i x + w
+ *   last    (shape [0,1]):     y  = a[d-1] D x + w + a_y y
+ * Only size-preserving BCs (periodic, free no-grow): every sweep re-reads
+ * the original x, so grow/shrink shapes cannot be chained.
+ * ====================================================================== */
+int oracle_d_kin(int d, const int *n, const int *bc, const double *x, double *y,
+                 double *w1, double *w2, const double *a, double a_x, double a_y)
+{
+    if (d < 1 || d > 16 || !n || !bc || !x || !y || !a) return E_ARG;
+    if (d > 1 && (!w1 || (d > 2 && !w2))) return E_ARG;
+    for (int i = 0; i < d; ++i) {
+        if (n[i] < 1) return E_ARG;
+        if (bc[i] != BC_PERIODIC && bc[i] != BC_FREE) return E_BC;
+    }
+    for (int i = 0; i < d; ++i) {
+        long nL = 1, nR = 1;
+        for (int j = 0; j < i; ++j) nL *= n[j];
+        for (int j = i + 1; j < d; ++j) nR *= n[j];
+        const double *x2;
+        double *dst;
+        if (d == 1) { x2 = 0; dst = y; }
+        else if (i == 0) { x2 = 0; dst = w1; }
+        else if (i == d - 1) { x2 = ((d - 1) % 2 == 1) ? w1 : w2; dst = y; }
+        else { x2 = (i % 2 == 1) ? w1 : w2; dst = (i % 2 == 1) ? w2 : w1; }
+        const int last = (i == d - 1);
+        ocall c = { (int)nL, n[i], (int)nR, 0, 0, 0, 0, x, x2, dst,
+                    1, a[i], i == 0, a_x, (last && a_y != 0.0) ? 1 : 0, a_y, 0 };
+        conv1d(&F_D2, bc[i], &c);
+    }
+    return OK;
+}

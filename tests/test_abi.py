@@ -1,0 +1,89 @@
+"""C-ABI library checks that need no GPU: it loads, exports every symbol the
+header declares, validates arguments before touching the device, and its
+cost model follows the reference formula (GenericConvolution2.rb:1269-1276,
+1525-1558, 1850-1932)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+
+def test_library_exports_every_declared_symbol(pkg):
+    L = pkg.lib()
+    names = pkg.declared_symbols()
+    assert len(names) >= 37
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    import subprocess
+    nm = subprocess.run(['nm', '-D', '--defined-only', pkg.LIB_PATH], capture_output=True, text=True)
+    if nm.returncode == 0:
+        exported = {l.split()[2] for l in nm.stdout.splitlines()
+                    if ' T ' in l and not l.split()[2].startswith('_Z')}
+        assert exported == set(names), exported ^ set(names)
+    assert pkg.lib().libconv_gb300_version().decode().startswith('libconv-gb300')
+
+
+def test_status_strings(pkg):
+    L = pkg.lib()
+    for code in (0, -1, -2, -3, -4, -5, -6):
+        assert L.libconv_gb300_strerror(code).decode() != 'unknown status'
+
+
+@pytest.mark.parametrize('bc,nx,ny,status', [
+    (7, 8, 8, -2),       # unknown BC
+    (1, 8, 8, -3),       # grow needs ny >= n + 15
+    (-1, 8, 8, -3),      # shrink needs nx >= n + 15
+    (0, 0, 8, -1),       # bad leading size
+])
+def test_argument_validation_before_device(pkg, bc, nx, ny, status):
+    x = np.zeros(1024)
+    y = np.zeros(1024)
+    with pytest.raises(pkg.LibconvError) as e:
+        pkg.Kernel('d_s0s0_1d_sym8_md').run(1, 0, [8], bc, [nx], [ny], 1, x, y, 1.0, 0.0, 0.0)
+    assert e.value.status == status
+    assert pkg.last_error() != ''
+
+
+def test_kinetic_rejects_grow(pkg):
+    x = np.zeros(512)
+    with pytest.raises(pkg.LibconvError) as e:
+        pkg.Kernel('d_kin').run(3, [8, 8, 8], [1, 0, 0], x, x.copy(), x.copy(), x.copy(),
+                                [1.0, 1.0, 1.0], 0.0, 0.0)
+    assert e.value.status == -2
+
+
+def test_mode_setting(pkg):
+    pkg.set_mode(pkg.MODE_FP64)
+    with pytest.raises(pkg.LibconvError):
+        pkg.set_mode(99)
+
+
+def test_cost_model(pkg):
+    n = [124, 132, 130]
+    N = int(np.prod(n))
+    # 1D: n[idim] * filter.cost * prod(other n) * narr
+    assert pkg.cost('d_s0s0_1d_sym8_md_cost', 3, 1, n, 0, 2) == 32 * N * 2
+    assert pkg.cost('d_s0s0_1d_sym8_d2_cost', 3, 0, n, 0, 1) == 58 * N
+    assert pkg.cost('d_s0s1_1d_sym8_cost', 3, 0, [62, 66, 65], 0, 1) == 62 * 64 * 66 * 65
+    # 3D periodic MagicFilter: 3 sweeps of 32 flop per point
+    assert pkg.cost('d_sfrf_cost', 3, n, [0, 0, 0], 1) == 96 * N
+    # grow: sizes grow sweep by sweep
+    g = [v + 15 for v in n]
+    want = 32 * (n[0] * n[1] * n[2] + n[1] * g[0] * n[2] + n[2] * g[0] * g[1])
+    assert pkg.cost('d_sfrf_cost', 3, n, [1, 1, 1], 1) == want
+    assert pkg.cost('d_kin_cost', 3, n, [0, 0, 0]) == 174 * N
+    # wavelets: n pairs * 64 * (2n)(2n) per sweep
+    m = [62, 66, 65]
+    assert pkg.cost('d_dwt_sym8_cost', 3, m, [0, 0, 0]) == 3 * 64 * 4 * int(np.prod(m))
+
+
+def test_declared_signatures_match_binding(pkg):
+    """Every 1D / 3D operator the header declares has a host and a _dev
+    export bound with the argument count of its reference procedure."""
+    declared = set(pkg.declared_symbols())
+    for name, args in pkg.SIGNATURES.items():
+        assert name in declared and name + '_dev' in declared
+    assert len(pkg.SIGNATURES['d_s0s0_1d_sym8_md']) == 12   # d,idim,n,bc,nx,ny,narr,x,y,a,a_x,a_y
+    assert len(pkg.SIGNATURES['d_s0s1_1d_sym8']) == 11      # ... a, a_y
+    assert len(pkg.SIGNATURES['d_sfrf_ld_narr']) == 10      # d,n,bc,nx,ny,narr,x,y,w1,w2
+    assert len(pkg.SIGNATURES['d_kin']) == 10               # d,n,bc,x,y,w1,w2,a,a_x,a_y
