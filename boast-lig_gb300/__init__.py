@@ -26,6 +26,7 @@ HEADER = os.path.join(HERE, '..', 'include', 'libconv_gb300.h')
 
 BC_SHRINK, BC_PERIODIC, BC_GROW, BC_FREE = -1, 0, 1, 2
 MODE_FP64 = 0
+MODE_TC_EXACT = 1
 
 _I = ctypes.POINTER(ctypes.c_int)
 _D = ctypes.POINTER(ctypes.c_double)
@@ -86,6 +87,8 @@ def lib():
         L.libconv_gb300_set_mode.argtypes = [_int]
         L.libconv_gb300_set_mode.restype = _int
         L.libconv_gb300_get_mode.restype = _int
+        L.libconv_gb300_check.argtypes = [_vp]
+        L.libconv_gb300_check.restype = _int
         _lib = L
     return _lib
 
@@ -99,6 +102,35 @@ def declared_symbols():
 
 def last_error():
     return lib().libconv_gb300_last_error().decode()
+
+
+def get_mode():
+    return lib().libconv_gb300_get_mode()
+
+
+class mode:
+    """Context manager: run the enclosed calls (this thread) in a compute mode."""
+
+    def __init__(self, m):
+        self.m = m
+
+    def __enter__(self):
+        self.old = get_mode()
+        set_mode(self.m)
+        return self
+
+    def __exit__(self, *exc):
+        set_mode(self.old)
+
+
+def check(stream=None):
+    """Synchronise and raise if a device-side wait of a *_dev call timed out."""
+    s = stream
+    if s is not None and not isinstance(s, int):
+        s = s.cuda_stream if hasattr(s, 'cuda_stream') else int(s)
+    st = lib().libconv_gb300_check(ctypes.c_void_p(s) if s else None)
+    if st:
+        raise LibconvError(st, 'libconv_gb300_check', last_error())
 
 
 def set_mode(mode):

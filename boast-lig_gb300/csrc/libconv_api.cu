@@ -15,6 +15,7 @@
 
 #include "../../include/libconv_gb300.h"
 #include "lcg_sweep.cuh"
+#include "lcg_tc.cuh"
 #include "libconv_filters.h"
 
 using namespace lcg;
@@ -50,6 +51,8 @@ struct OpDef {
 #define CONV_OP(TAB, NT, LOW) { KCONV, {TAB, TAB}, {NT, NT}, {LOW, LOW}, NT, 2 * NT }
 #define WT_OP(KIND, P, GS) { KIND, {LCG_FTAB_##P, LCG_FTAB_##GS}, {LCG_##P##_NTAPS, LCG_##GS##_NTAPS}, \
         {LCG_##P##_LOWFIL, LCG_##GS##_LOWFIL}, LCG_##P##_LENGTH, 4 * LCG_##P##_LENGTH }
+
+const double h_ftab[LCG_FTAB_N] = LCG_FTAB_INIT;
 
 const OpDef OP_MD = CONV_OP(LCG_FTAB_MD, 16, LCG_CONV_SYM8_MD_LOWFIL);
 const OpDef OP_IMD = CONV_OP(LCG_FTAB_IMD, 16, LCG_CONV_SYM8_IMD_LOWFIL);
@@ -107,6 +110,7 @@ struct DevState {
     DevBuf buf[6];                   // x, y, w1, w2, dot partials, dot scalar
     DevBuf scratch;                  // dot partials of the *_dev entry points
     DevBuf dscalar;
+    DevBuf status;                   // device status word (bounded waits)
 };
 
 std::mutex g_mu;
@@ -142,6 +146,9 @@ DevState *dev_state(int &rc) {
     if (!s.init) {
         cudaError_t e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) { rc = cuda_fail(e, "cudaStreamCreate"); return nullptr; }
+        if ((rc = ensure(s.status, sizeof(int)))) return nullptr;
+        e = cudaMemset(s.status.p, 0, sizeof(int));
+        if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemset"); return nullptr; }
         s.init = true;
     }
     return &s;
@@ -306,8 +313,9 @@ int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, do
 // Launch the plan's sweeps with bound device pointers.  dot_dev receives the
 // dot product (device) when the plan has one; `scratch` holds the partials.
 int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, double *dot_dev,
-             cudaStream_t st) {
-    if (t_mode != LIBCONV_MODE_FP64) return fail(LIBCONV_EMODE, "unknown mode %d", t_mode);
+             int *status, cudaStream_t st) {
+    if (t_mode != LIBCONV_MODE_FP64 && t_mode != LIBCONV_MODE_TC_EXACT)
+        return fail(LIBCONV_EMODE, "unknown mode %d", t_mode);
     for (const PlanStep &ps : P.steps) {
         Sweep S = ps.S;
         S.x = bufs[ps.src];
@@ -315,14 +323,22 @@ int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, double *dot_
         S.x2 = ps.src2 >= 0 ? bufs[ps.src2] : nullptr;
         if (!S.x || !S.y || (ps.src2 >= 0 && !S.x2))
             return fail(LIBCONV_EARG, "null device buffer in plan");
+        const bool tc = t_mode == LIBCONV_MODE_TC_EXACT && sweep_tc_supported(S);
         long long nb = 0;
         if (S.has_dot) {
-            nb = sweep_fp64_blocks(S);
+            nb = tc ? sweep_tc_blocks(S) : sweep_fp64_blocks(S);
             int rc = ensure(scratch, (size_t)nb * sizeof(double));
             if (rc) return rc;
             S.dot_part = (double *)scratch.p;
         }
-        cudaError_t e = launch_sweep_fp64(S, st);
+        cudaError_t e;
+        if (tc) {
+            TcFilter F;
+            tc_filter_digits(h_ftab + S.ftab, S.ntaps, F);
+            e = launch_sweep_tc(S, F, status, st);
+        } else {
+            e = launch_sweep_fp64(S, st);
+        }
         if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
         if (S.has_dot) {
             e = launch_dot_reduce(S.dot_part, nb, dot_dev, 0, st);
@@ -344,7 +360,19 @@ int exec_dev(const Plan &P, const double *x, double *y, double *w1, double *w2, 
     int rc;
     DevState *s = dev_state(rc);
     if (!s) return rc;
-    return run_plan(P, bufs, s->scratch, dot_dev, (cudaStream_t)stream);
+    return run_plan(P, bufs, s->scratch, dot_dev, (int *)s->status.p, (cudaStream_t)stream);
+}
+
+// Read and clear the device status word (after the work was synchronised).
+int read_status(DevState &s) {
+    int v = 0;
+    cudaError_t e = cudaMemcpy(&v, s.status.p, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "read status");
+    if (v) {
+        cudaMemset(s.status.p, 0, sizeof(int));
+        return fail(LIBCONV_ETIMEOUT, "a tensor-core wait timed out on the device (status %d)", v);
+    }
+    return LIBCONV_OK;
 }
 
 // Host-pointer execution: stage in device buffers owned by the library.
@@ -368,7 +396,8 @@ int exec_host(const Plan &P, const double *x, double *y, double *dot_host) {
         e = cudaMemcpyAsync(bufs[B_Y], y, P.y_read * sizeof(double), cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) return cuda_fail(e, "copy y to device");
     }
-    rc = run_plan(P, bufs, s->scratch, P.has_dot ? (double *)s->dscalar.p : nullptr, st);
+    rc = run_plan(P, bufs, s->scratch, P.has_dot ? (double *)s->dscalar.p : nullptr,
+                  (int *)s->status.p, st);
     if (rc) return rc;
     e = cudaMemcpyAsync(y, bufs[B_Y], P.elems[B_Y] * sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e != cudaSuccess) return cuda_fail(e, "copy y to host");
@@ -378,7 +407,7 @@ int exec_host(const Plan &P, const double *x, double *y, double *dot_host) {
     }
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "synchronize");
-    return LIBCONV_OK;
+    return read_status(*s);
 }
 
 // ---- cost model (GenericConvolution2.rb:1269-1276, 1525-1558, 1850-1932) ----
@@ -430,14 +459,26 @@ const char *libconv_gb300_strerror(int s) {
     case LIBCONV_ECUDA: return "CUDA error";
     case LIBCONV_ENOMEM: return "device allocation failed";
     case LIBCONV_EMODE: return "unknown compute mode";
+    case LIBCONV_ETIMEOUT: return "device-side wait timed out";
     default: return "unknown status";
     }
 }
 
 const char *libconv_gb300_last_error(void) { return t_err.c_str(); }
 
+int libconv_gb300_check(void *stream) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    int rc;
+    DevState *s = dev_state(rc);
+    if (!s) return rc;
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "synchronize");
+    return read_status(*s);
+}
+
 int libconv_gb300_set_mode(int mode) {
-    if (mode != LIBCONV_MODE_FP64) return fail(LIBCONV_EMODE, "unknown mode %d", mode);
+    if (mode != LIBCONV_MODE_FP64 && mode != LIBCONV_MODE_TC_EXACT)
+        return fail(LIBCONV_EMODE, "unknown mode %d", mode);
     t_mode = mode;
     return LIBCONV_OK;
 }

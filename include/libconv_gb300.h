@@ -38,6 +38,7 @@ extern "C" {
 #define LIBCONV_ECUDA    -4   /* CUDA runtime error (message in libconv_gb300_last_error) */
 #define LIBCONV_ENOMEM   -5   /* device allocation failed */
 #define LIBCONV_EMODE    -6   /* unknown compute mode */
+#define LIBCONV_ETIMEOUT -7   /* a bounded device-side wait gave up (status word set) */
 
 #define LIBCONV_BC_SHRINK   -1
 #define LIBCONV_BC_PERIODIC  0
@@ -45,8 +46,13 @@ extern "C" {
 #define LIBCONV_BC_FREE      2
 
 /* Compute modes for libconv_gb300_set_mode (per calling thread).
- *   FP64: plain FP64 FMA kernels on the CUDA cores (default). */
-#define LIBCONV_MODE_FP64   0
+ *   FP64:     plain FP64 FMA kernels on the CUDA cores (default).
+ *   TC_EXACT: MagicFilter / kinetic / derivative sweeps on the tcgen05 tensor
+ *             cores with exact integer digit arithmetic (FP16 digits, FP32
+ *             accumulation kept exact); FP64-class accuracy. Wavelet sweeps
+ *             run the FP64 kernels in this mode. */
+#define LIBCONV_MODE_FP64      0
+#define LIBCONV_MODE_TC_EXACT  1
 
 const char *libconv_gb300_version(void);
 const char *libconv_gb300_strerror(int status);
@@ -54,6 +60,10 @@ const char *libconv_gb300_strerror(int status);
 const char *libconv_gb300_last_error(void);
 int libconv_gb300_set_mode(int mode);
 int libconv_gb300_get_mode(void);
+/* Synchronise `stream` (void* cudaStream_t) and report LIBCONV_ETIMEOUT if a
+ * device-side wait of an earlier *_dev call on this device gave up; clears
+ * the device status word. */
+int libconv_gb300_check(void *stream);
 
 /* ---------------------------------------------------------------------
  * 1D sweeps: GenericConvolutionOperator1d#procedure

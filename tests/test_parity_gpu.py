@@ -14,6 +14,15 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-13
 
 
+@pytest.fixture(autouse=True, params=['fp64', 'tc_exact'])
+def compute_mode(request, pkg):
+    """Every parity case runs with the FP64 kernels and with the tensor-core
+    exact-digit kernels (wavelet sweeps use the FP64 kernels in both)."""
+    m = pkg.MODE_FP64 if request.param == 'fp64' else pkg.MODE_TC_EXACT
+    with pkg.mode(m):
+        yield request.param
+
+
 def rel(a, b):
     return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
 
