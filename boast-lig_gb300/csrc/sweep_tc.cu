@@ -1,9 +1,12 @@
 // FP64-accurate convolution sweep on the tcgen05 tensor cores.
 //
 // Exact integer arithmetic on FP16 operands:
-//   * a tile of 128 lines x KT input positions is scaled by one power of two
-//     (the tile's largest exponent) to integers X with |X| < 2^62, and X is cut
-//     into 7 balanced base-512 digits d_0..d_6 (|d| <= 256, exact in FP16);
+//   * each line of a 128-line x KT-position tile is scaled by one power of two
+//     (the line segment's largest exponent) to integers X with |X| < 2^62, and
+//     X is cut into 7 balanced base-512 digits d_0..d_6 (|d| <= 256, exact in
+//     FP16).  Lines never share a scale, so a line's result does not depend on
+//     the magnitudes of the other lines of its tile; a line segment holding an
+//     Inf or NaN yields NaN for the outputs of that tile row;
 //   * the filter taps are scaled by the power of two above their largest
 //     magnitude and cut the same way into digits e_0..e_6;
 //   * every digit-pair product is an integer of magnitude <= 2^16 and every
@@ -59,7 +62,7 @@ template <int NT> struct TcGeom {
     static constexpr int B_PLANE = 16 * KB * 2;
     static constexpr int A_BYTES = kS * A_PLANE;
     static constexpr int B_BYTES = kS * B_PLANE;
-    static constexpr int SMEM = A_BYTES + B_BYTES + 256 + 1024;  // + barrier/slots + alignment
+    static constexpr int SMEM = A_BYTES + B_BYTES + 256 + 4 * kM + 1024;  // + slots, row exponents, alignment
 };
 
 // ---- PTX wrappers ----------------------------------------------------------------
@@ -160,8 +163,8 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
     uint8_t *B = smem + G::A_BYTES;
     uint64_t *bar = (uint64_t *)(B + G::B_BYTES);
     uint32_t *tslot = (uint32_t *)(bar + 1);
-    int *emax = (int *)(tslot + 1);
     double *red = (double *)(tslot + 4);   // 8 doubles, 8-byte aligned
+    int *rowmax = (int *)(red + 8);        // largest biased exponent of each tile row
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int arr = blockIdx.z;
@@ -185,8 +188,8 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-        *emax = 0;
     }
+    for (int i = tid; i < kM; i += kThreads) rowmax[i] = 0;
 
     // ---- Toeplitz filter tiles B_t[n][kk] = e_t(kk - n), K-major core matrices
     for (int idx = tid; idx < kS * 16 * G::KB; idx += kThreads) {
@@ -199,7 +202,8 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
     }
     __syncthreads();
 
-    // ---- pass 1: largest exponent of the tile
+    // ---- pass 1: largest exponent of each line segment (a thread always owns
+    // the same row: row = tid % 128)
     constexpr int kChunks = G::KT / 8;
     int mx = 0;
     for (int id = tid; id < kM * kChunks; id += kThreads) {
@@ -217,10 +221,9 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
             }
         }
     }
-    mx = __reduce_max_sync(0xffffffffu, mx);
-    if (lane == 0) atomicMax(emax, mx);
+    atomicMax(&rowmax[tid % kM], mx);
     __syncthreads();
-    const int E = (*emax ? *emax : 1) - 1022;   // |x| < 2^E over the tile
+    const int E = (rowmax[tid % kM] ? rowmax[tid % kM] : 1) - 1022;   // |x| < 2^E on the row
 
     // ---- pass 2: digit planes, 8 positions (one core-matrix row) per task
     for (int id = tid; id < kM * kChunks; id += kThreads) {
@@ -292,7 +295,9 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
     const long long g = g0 + row;
     const long long l = g % S.nL, rr = g / S.nL;
     const long long out_ext = S.out_ext;
-    const double scale = (S.has_a ? S.a : 1.0) * ldexp(1.0, E + F.ef - 61);
+    const int rmax = rowmax[row];
+    const double scale = rmax == 0x7FF ? __longlong_as_double(0x7FF8000000000000LL)
+                                       : (S.has_a ? S.a : 1.0) * ldexp(1.0, (rmax ? rmax : 1) - 1022 + F.ef - 61);
     double dot = 0.0;
     for (int jj = 0; jj < kNB / 2; ++jj) {
         const int j = jb * (kNB / 2) + jj;

@@ -65,3 +65,24 @@ def test_tc_accuracy_vs_exact(tc, O, op, taps_name, lowfil, a):
     e_tc, e_64 = rel(y, ex), rel(y64, ex)
     assert e_tc <= 1e-13
     assert e_tc <= max(2 * e_64, 1e-15), (e_tc, e_64)
+
+
+def test_tc_lines_do_not_share_a_scale(tc, O):
+    """A line of huge values or a NaN in the same 128-line tile must not change
+    the other lines' results (each line segment has its own power-of-two scale)."""
+    from boast_lig_gb300 import inputs
+    n, ndat = 48, 100
+    x = inputs.uniform(9, n * ndat)
+    x[3 * n:4 * n] *= 1e200          # line 3: huge
+    x[7 * n + 5] = np.nan             # line 7: one NaN
+    x[11 * n:12 * n] *= 1e-200        # line 11: tiny
+    y = np.zeros_like(x)
+    tc.Kernel('d_s0s0_1d_sym8_md').run(1, 0, [n], 0, [n], [n], ndat, x, y, 1.0, 0.0, 0.0)
+    yo = np.zeros_like(x)
+    O.call('oracle_d_s0s0_1d_sym8_md', 1, 0, [n], 0, [n], [n], ndat, x, yo, 1.0, 0.0, 0.0)
+    Y, R = y.reshape(ndat, n), yo.reshape(ndat, n)
+    assert np.all(np.isnan(Y[7]))
+    for r in range(ndat):
+        if r == 7:
+            continue
+        assert rel(Y[r], R[r]) <= 1e-13, r
