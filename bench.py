@@ -189,8 +189,10 @@ def run_gpu(args):
     w1 = torch.empty(B * N, dtype=torch.float64, device=dev)
     w2 = torch.empty(B * N, dtype=torch.float64, device=dev)
     a = [-0.5 / HGRID ** 2] * 3
+    tc = args.mode == 'tc_exact'
+    pkg.set_mode(pkg.MODE_TC_EXACT if tc else pkg.MODE_FP64)
     mf = pkg.Kernel('d_sfrf_ld_narr')
-    kin = pkg.Kernel('d_kin')
+    kin = pkg.Kernel('d_kin_narr')
     stream = torch.cuda.Stream(device=dev)
     sp = stream.cuda_stream
     base_ptr = xd.data_ptr()
@@ -201,10 +203,7 @@ def run_gpu(args):
         mf.run_dev(3, n, [0, 0, 0], n, n, B, xd, psir, w1, w2, stream=sp)
         if evs:
             evs[1].record(stream)
-        for b in range(B):
-            off = b * N * 8
-            kin.run_dev(3, n, [0, 0, 0], base_ptr + off, tx.data_ptr() + off, w1.data_ptr() + off,
-                        w2.data_ptr() + off, a, 0.0, 0.0, stream=sp)
+        kin.run_dev(3, n, [0, 0, 0], B, xd, tx, w1, w2, a, 0.0, 0.0, stream=sp)
         if evs:
             evs[2].record(stream)
 
@@ -249,9 +248,7 @@ def run_gpu(args):
 
     def e2e_step():
         mf.run(3, n, [0, 0, 0], n, n, B, hx, host_psir, hw, hw)
-        for b in range(B):
-            kin.run(3, n, [0, 0, 0], hx[b * N:(b + 1) * N], host_tx[b * N:(b + 1) * N], hw, hw,
-                    a, 0.0, 0.0)
+        kin.run(3, n, [0, 0, 0], B, hx, host_tx, hw, hw, a, 0.0, 0.0)
 
     e2e_step()
     barrier()
@@ -264,39 +261,48 @@ def run_gpu(args):
     e_t = (time.perf_counter() - t0) / e_steps
     e2e = {'value': pts_step / e_t, 'unit': UNIT, 'h2d_bytes_per_step': 2 * B * N * 8,
            'd2h_bytes_per_step': 2 * B * N * 8,
-           'note': 'd_sfrf_ld_narr (narr=B) + d_kin per grid, host pointers (pinned), '
+           'note': 'd_sfrf_ld_narr (narr=B) + d_kin_narr (narr=B), host pointers (pinned), '
                    'H2D of x and D2H of psi_r and T x inside every call'}
 
     # roofline of the dominant kernel (kinetic sweep, 29 taps): 3 launches per
     # grid; algorithmic bytes per grid 64 B/pt (16 + 24 + 24)
     hbm, src = peaks()
-    launches_kin = 3 * B * args.steps
+    launches_kin = 3 * args.steps
     t_launch = kin_ms / 1e3 / launches_kin
-    bytes_launch = 64.0 / 3.0 * N
+    bytes_launch = 64.0 / 3.0 * N * B
     achieved = bytes_launch / t_launch / 1e9
-    flops_launch = (58 + 1 + 2.0 / 3.0) * N     # 29 FMA, scale, x2 add (2 of 3 sweeps)
+    flops_launch = (58 + 1 + 2.0 / 3.0) * N * B  # 29 FMA, scale, x2 add (2 of 3 sweeps)
     traffic = None
-    tp = os.path.join(ROOT, 'profiles', 'kinetic_sweep_fp64_traffic.json')
+    kname = ('sweep_tc_kernel<29> (kinetic sweep, all grids per launch)' if tc
+             else 'sweep_fp64_kernel<KCONV,29> (kinetic sweep, all grids per launch)')
+    tp = os.path.join(ROOT, 'profiles', ('kinetic_sweep_tc_traffic.json' if tc
+                                         else 'kinetic_sweep_fp64_traffic.json'))
     if os.path.exists(tp):
         tj = json.load(open(tp))
-        traffic = tj['dram_bytes_per_point'] * N
+        traffic = tj['dram_bytes_per_point'] * N * B
     roof = {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
-            'frac': achieved / hbm, 'traffic': traffic,
-            'kernel': 'sweep_fp64_kernel<KCONV,29> (kinetic sweep)',
-            'peak_source': src,
-            'fp64_pipe': {'achieved_tflops': flops_launch / t_launch / 1e12,
-                          'nominal_peak_tflops': 1.25,
-                          'note': 'plain FP64 FMA path: bound by the FP64 pipe, not HBM'}}
+            'frac': achieved / hbm, 'traffic': traffic, 'kernel': kname, 'peak_source': src}
+    if tc:
+        # tensor work per output: 28 digit pairs x K=48 x 2 flops (not algorithmic flops)
+        bf = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))).get('bf16_tflops', 1900.0) \
+            if os.path.exists(os.path.join(ROOT, 'MEASURED_PEAKS.json')) else 1900.0
+        tflops = 36 * 48 * 2 * N * B / t_launch / 1e12
+        roof['tensor_pipe'] = {'mma_tflops': tflops, 'peak_tflops': bf, 'frac': tflops / bf,
+                               'note': 'exact FP16-digit MMAs (36 byte pairs, K=48 per 16 outputs)'}
+    else:
+        roof['fp64_pipe'] = {'achieved_tflops': flops_launch / t_launch / 1e12,
+                             'nominal_peak_tflops': 1.25,
+                             'note': 'plain FP64 FMA path: bound by the FP64 pipe, not HBM'}
     line = {'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
             'warmup': max(args.warmup, 3), 'ms_per_step': ms / args.steps, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
             'data': 'synthetic (seeded Gaussian-filtered noise, sigma=2, unit RMS)',
             'config': {'workload': f'{B} grids of 128^3 periodic per GPU per step: '
-                                   'MagicFilter3D (d_sfrf_ld_narr) + Kinetic3D (d_kin, h=0.45)',
-                       'grid': n, 'grids_per_gpu': B, 'mode': 'fp64',
+                                   'MagicFilter3D (d_sfrf_ld_narr) + Kinetic3D (d_kin_narr, h=0.45)',
+                       'grid': n, 'grids_per_gpu': B, 'mode': args.mode,
                        'l2': 'inputs larger than L2 (537 MB per array)',
                        'ms_magicfilter3d': mf_ms / args.steps, 'ms_kinetic3d': kin_ms / args.steps},
-            'clocks': ck, 'e2e': e2e, 'gpu_launches': args.steps * (3 + 3 * B),
+            'clocks': ck, 'e2e': e2e, 'gpu_launches': args.steps * 6,
             'roofline': roof}
     if rank == 0 and world == 1 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline_sample(base)
@@ -315,6 +321,8 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--grids', type=int, default=32)
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline sample')
+    ap.add_argument('--mode', default='tc_exact', choices=['tc_exact', 'fp64'],
+                    help='tc_exact: tensor-core exact-digit sweeps (FP64-accurate); fp64: FP64 FMA')
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)

@@ -6,17 +6,17 @@
 
 namespace lcg {
 
-// Balanced base-512 digits of the fixed-point filter, as FP16 bit patterns:
-// tap value = 2^(ef-62) * sum_s dig[s] 512^(6-s).
+// Signed byte digits of the 64-bit fixed-point filter (operator scalar folded
+// in exactly), as FP16 bit patterns: a*tap = 2^(ef-64) * sum_s dig[s] 256^(7-s).
 struct TcFilter {
-    static constexpr int kSlices = 7;
+    static constexpr int kSlices = 8;
     static constexpr int kMaxTaps = 32;
     unsigned short dig[kSlices][kMaxTaps];
     int ef;
 };
 
-// Host: digits of taps[0..ntaps).
-void tc_filter_digits(const double *taps, int ntaps, TcFilter &F);
+// Host: digits of a * taps[0..ntaps).
+void tc_filter_digits(const double *taps, int ntaps, double a, TcFilter &F);
 bool sweep_tc_supported(const Sweep &S);
 long long sweep_tc_blocks(const Sweep &S);
 // status (device int) is set non-zero if a tensor-core wait timed out.

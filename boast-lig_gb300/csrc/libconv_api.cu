@@ -268,9 +268,11 @@ int plan_md_t(const OpDef &op, int d, const int *n, const int *bc, const int *nx
     return LIBCONV_OK;
 }
 
-// Multi-D kinetic, transpose = 0 (Kinetic2.rb:1068-1090).
+// Multi-D kinetic, transpose = 0 (Kinetic2.rb:1068-1090), over narr grids
+// laid back to back (narr = 1 is the reference's Kinetic()).
 int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, double a_y,
-             Plan &P) {
+             Plan &P, int narr = 1) {
+    if (narr < 1 || narr > 65535) return fail(LIBCONV_EARG, "narr=%d out of [1,65535]", narr);
     if (d < 1 || d > 16) return fail(LIBCONV_EARG, "d=%d out of [1,16]", d);
     if (!n || !bc || !a) return fail(LIBCONV_EARG, "n/bc/a must not be null");
     long long tot = 1;
@@ -300,12 +302,14 @@ int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, do
         st.src = B_X;
         st.dst = t;
         st.src2 = i == 0 ? -1 : s;
-        need(P, B_X, tot);
-        need(P, t, tot);
-        if (st.src2 >= 0) need(P, st.src2, tot);
+        st.S.narr = narr;
+        st.S.x_arr = st.S.y_arr = tot;
+        need(P, B_X, tot * narr);
+        need(P, t, tot * narr);
+        if (st.src2 >= 0) need(P, st.src2, tot * narr);
         P.steps.push_back(st);
     }
-    P.y_read = a_y != 0.0 ? tot : 0;
+    P.y_read = a_y != 0.0 ? tot * narr : 0;
     return LIBCONV_OK;
 }
 
@@ -334,7 +338,8 @@ int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, double *dot_
         cudaError_t e;
         if (tc) {
             TcFilter F;
-            tc_filter_digits(h_ftab + S.ftab, S.ntaps, F);
+            tc_filter_digits(h_ftab + S.ftab, S.ntaps, S.has_a ? S.a : 1.0, F);
+            S.has_a = 0;   // folded exactly into the filter digits
             e = launch_sweep_tc(S, F, status, st);
         } else {
             e = launch_sweep_fp64(S, st);
@@ -592,6 +597,20 @@ int d_kin_dev(int d, const int *n, const int *bc, const double *x, double *y, do
               double *w2, const double *a, double a_x, double a_y, void *stream) {
     Plan P;
     int rc = plan_kin(d, n, bc, a, a_x, a_y, P);
+    return rc ? rc : exec_dev(P, x, y, w1, w2, nullptr, stream);
+}
+
+int d_kin_narr(int d, const int *n, const int *bc, int narr, const double *x, double *y,
+               double *w1, double *w2, const double *a, double a_x, double a_y) {
+    (void)w1; (void)w2;
+    Plan P;
+    int rc = plan_kin(d, n, bc, a, a_x, a_y, P, narr);
+    return rc ? rc : exec_host(P, x, y, nullptr);
+}
+int d_kin_narr_dev(int d, const int *n, const int *bc, int narr, const double *x, double *y,
+                   double *w1, double *w2, const double *a, double a_x, double a_y, void *stream) {
+    Plan P;
+    int rc = plan_kin(d, n, bc, a, a_x, a_y, P, narr);
     return rc ? rc : exec_dev(P, x, y, w1, w2, nullptr, stream);
 }
 

@@ -1,30 +1,42 @@
 // FP64-accurate convolution sweep on the tcgen05 tensor cores.
 //
-// Exact integer arithmetic on FP16 operands:
-//   * each line of a 128-line x KT-position tile is scaled by one power of two
-//     (the line segment's largest exponent) to integers X with |X| < 2^62, and
-//     X is cut into 7 balanced base-512 digits d_0..d_6 (|d| <= 256, exact in
-//     FP16).  Lines never share a scale, so a line's result does not depend on
-//     the magnitudes of the other lines of its tile; a line segment holding an
-//     Inf or NaN yields NaN for the outputs of that tile row;
-//   * the filter taps are scaled by the power of two above their largest
-//     magnitude and cut the same way into digits e_0..e_6;
-//   * every digit-pair product is an integer of magnitude <= 2^16 and every
-//     partial sum over <= 29 taps x 7 pairs stays below 2^24, so the FP32
-//     accumulation of tcgen05.mma (kind::f16) is exact;
-//   * the pairs of order k = s + t <= 5 (21 pairs) and of order 6 (all 7 for
-//     the 29-tap filters, whose large alternating taps cancel; the leading
-//     (0,6) and (6,0) for the 16-tap MagicFilter) are accumulated in TMEM, one
-//     accumulator per order; the epilogue recombines
-//     Y = sum_{k<=5} Acc_k 512^(5-k) + Acc_6 / 512 in int64 and scales it back
-//     to FP64 together with the operator scalar a.
-// The dropped orders weigh <= 2^-63 of the tile scale: the result is at least
-// as accurate as the FP64 FMA chain.
+// Exact integer arithmetic on FP16 operands
+//   * each line segment of a tile (128 lines x KT positions) is scaled by the
+//     power of two above its largest magnitude to 64-bit integers |X| < 2^64;
+//     the 8 bytes of |X| are the digits d_0 (top byte) .. d_7, each held
+//     exactly in FP16 with the sign of x;
+//   * the filter, with the operator scalar a folded in exactly (128-bit
+//     product of the two mantissas), is cut the same way into bytes e_0..e_7;
+//   * every byte-pair product is below 2^16 and every partial sum over <= 29
+//     taps x 8 pairs stays below 2^24, so the FP32 accumulation of
+//     tcgen05.mma (kind::f16) is exact;
+//   * the pairs of order k = s + t <= 6 (16-tap MagicFilter: 28 pairs) or
+//     k <= 7 (29-tap kinetic / derivative filters, whose large alternating
+//     taps cancel: 36 pairs) are accumulated in TMEM, one accumulator per
+//     order; the epilogue recombines
+//        Y = sum_{k<=5} Acc_k 2^(8(5-k)) + Acc_6 / 2^8 + Acc_7 / 2^16
+//     in int64 and builds the FP64 result bit by bit (no FP64 instruction).
+//   Dropped orders weigh <= 2^-64 of the line scale: the result is at least as
+//   accurate as an FP64 FMA chain.  Lines never share a scale; a line segment
+//   holding an Inf or NaN gives NaN on that tile row.
 //
 // The convolution of one 16-output block is a banded Toeplitz product
 //   D[line, n] = sum_kk A[line, kk] * B[kk, n],   B[kk, n] = f(kk - n + lowfil)
 // with K = 32 (16 taps) or 48 (29 taps); A is a digit plane of the tile,
 // addressed at an offset of 16 positions per output block.
+//
+// Persistent, warp-specialised CTA (one per SM), single A buffer and single
+// TMEM accumulator set, 256 threads:
+//   warps 0-3  producers: largest exponent of each row segment, then its
+//              byte digits into the A planes (contiguous lines: one warp per
+//              row, lanes across positions; strided lines: one thread per row,
+//              lanes across consecutive lines; both coalesced);
+//   warps 4-7  epilogue: thread = TMEM lane = tile row; TMEM -> FP64 -> global;
+//              warp 4 also allocates TMEM and, once the epilogue has released
+//              the accumulators of tile i, issues the MMAs of tile i+1 (lane 0).
+// Producers fill tile i+1 while the epilogue drains tile i.  Every hand-off is
+// an mbarrier whose phase can never run two phases ahead of its waiter, and
+// every wait gives up after ~2 s of SM clock (status word set, TMEM freed).
 #include <cuda_fp16.h>
 #include <stdint.h>
 
@@ -35,34 +47,24 @@ namespace lcg {
 namespace {
 
 constexpr int kM = 128;          // lines per tile (MMA M)
-constexpr int kQC = 64;          // outputs per tile (4 blocks of N = 16)
-constexpr int kNB = kQC / 16;
-constexpr int kS = TcFilter::kSlices;   // digits per operand (7)
-constexpr int kG = 7;                   // accumulated orders k = 0..6
-
-// Digit pairs (s, t) accumulated, in issue order; order 6 is complete for the
-// 29-tap filters and reduced to its two leading pairs for 16 taps.
-template <int NT> struct Pairs {
-    static constexpr int N = NT > 16 ? 28 : 23;
-};
-__host__ __device__ constexpr int pair_s(int NT, int i) {
-    return i < 21 ? (i < 1 ? 0 : i < 3 ? i - 1 : i < 6 ? i - 3 : i < 10 ? i - 6 : i < 15 ? i - 10 : i - 15)
-                  : (NT > 16 ? i - 21 : (i == 21 ? 0 : 6));
-}
-__host__ __device__ constexpr int pair_k(int NT, int i) {
-    return i < 1 ? 0 : i < 3 ? 1 : i < 6 ? 2 : i < 10 ? 3 : i < 15 ? 4 : i < 21 ? 5 : 6;
-}
+constexpr int kQC = 64;          // outputs per tile
+constexpr int kNB = kQC / 16;    // 16-output blocks per tile
 constexpr int kThreads = 256;
 constexpr uint32_t kTmemCols = 512;
+constexpr long long kWaitCycles = 4000000000LL;
 
 template <int NT> struct TcGeom {
     static constexpr int KB = ((16 + NT - 1) + 15) / 16 * 16;   // K per output block
     static constexpr int KT = 16 * (kNB - 1) + KB;              // positions per tile
-    static constexpr int A_PLANE = kM * KT * 2;                 // bytes per digit plane
+    static constexpr int ORD = NT > 16 ? 8 : 7;                 // accumulated orders
+    static constexpr int ND = NT > 16 ? 8 : 7;                  // digit planes used
+    static constexpr int A_PLANE = kM * KT * 2;
     static constexpr int B_PLANE = 16 * KB * 2;
-    static constexpr int A_BYTES = kS * A_PLANE;
-    static constexpr int B_BYTES = kS * B_PLANE;
-    static constexpr int SMEM = A_BYTES + B_BYTES + 256 + 4 * kM + 1024;  // + slots, row exponents, alignment
+    static constexpr int A_BYTES = ND * A_PLANE;
+    static constexpr int B_BYTES = ND * B_PLANE;
+    static constexpr int AUX = 1024 + 2 * 4 * kM;               // barriers, slots, row exponents
+    static constexpr int SMEM = A_BYTES + B_BYTES + AUX + 1024;
+    static_assert(ORD * kNB * 16 <= (int)kTmemCols, "TMEM columns");
 };
 
 // ---- PTX wrappers ----------------------------------------------------------------
@@ -89,7 +91,23 @@ __device__ __forceinline__ void mma_f16(uint32_t d, uint64_t a, uint64_t b, uint
         : "memory");
 }
 
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ void commit(uint32_t bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void bar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void bar_arrive(uint32_t bar) {
+    asm volatile(
+        "{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -98,6 +116,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
         : "r"(bar), "r"(parity)
         : "memory");
     return ok != 0;
+}
+
+// Bounded wait for the phase of the given parity; false after ~2 s.
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
+    if (bar_try(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!bar_try(bar, parity))
+        if (clock64() - t0 > kWaitCycles) return false;
+    return true;
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
@@ -116,42 +143,60 @@ __device__ __forceinline__ int imod(int a, int n) {
     return r < 0 ? r + n : r;
 }
 
-// Input element of line g at logical processed index p (conv filters), with
-// the boundary condition applied; 0 outside the data of a free boundary.
-__device__ __forceinline__ double fetch_conv(const Sweep &S, const double *__restrict__ x,
-                                             long long g, int p) {
-    int pos;
-    if (S.bc == BC_PERIODIC) pos = imod(p, S.n);
-    else if (S.bc == BC_SHRINK) pos = p - S.in_lo;
-    else {
-        if (p < 0 || p >= S.n) return 0.0;
-        pos = p;
-    }
-    const long long l = g % S.nL, r = g / S.nL;
-    return x[l + (long long)S.nL * ((long long)pos + (long long)S.in_ext * r)];
+__device__ __noinline__ double scaled_slow(long long Y, int se) { return ldexp((double)Y, se); }
+
+// int64 Y times 2^se as an FP64, rounded to nearest even, built from the bits.
+__device__ __forceinline__ double scaled_to_f64(long long Y, int se) {
+    if (Y == 0) return 0.0;
+    const unsigned long long neg = Y < 0 ? (1ull << 63) : 0ull;
+    unsigned long long m = Y < 0 ? (unsigned long long)(-Y) : (unsigned long long)Y;
+    const int lz = __clzll((long long)m);
+    m <<= lz;
+    unsigned long long mant = m >> 11;
+    const unsigned rem = (unsigned)(m & 0x7FF);
+    mant += (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+    int e = 63 - lz + se;
+    if (mant >> 53) { mant >>= 1; ++e; }
+    if (e < -1022 || e > 1023) return scaled_slow(Y, se);    // outside the normal range
+    return __longlong_as_double((long long)(neg | ((unsigned long long)(e + 1023) << 52) |
+                                            (mant & 0xFFFFFFFFFFFFFull)));
 }
 
-// Balanced base-512 digits of X = round(x 2^(62-E)) (|x| < 2^E, |X| < 2^62).
-__device__ __forceinline__ void digits(double x, int E, int (&d)[kS]) {
-    const long long bits = __double_as_longlong(x);
+
+// Fixed-point magnitude |X| = round(|x| 2^(64-E)) of the FP64 bit pattern
+// (|x| < 2^E), split in 32-bit words, and the sign bit.  Integer only.
+__device__ __forceinline__ void fixed64(long long bits, int E, uint32_t &xl, uint32_t &xh,
+                                        uint32_t &sgn) {
     int ex = (int)((bits >> 52) & 0x7FF);
-    long long mant = bits & 0xFFFFFFFFFFFFFLL;
-    if (ex) mant |= 1LL << 52;
+    unsigned long long mant = (unsigned long long)bits & 0xFFFFFFFFFFFFFull;
+    if (ex) mant |= 1ull << 52;
     else ex = 1;
-    const int r = E - (ex - 1022) - 9;      // X = mant * 2^-r
-    long long X;
-    if (r <= 0) X = mant << (-r);
-    else if (r >= 63) X = 0;
-    else X = (mant + (1LL << (r - 1))) >> r;
-    if (bits < 0) X = -X;
-#pragma unroll
-    for (int s = kS - 1; s >= 1; --s) {
-        const long long u = X + 256;
-        d[s] = (int)(u & 511) - 256;
-        X = u >> 9;
-    }
-    d[0] = (int)X;
+    const int r = E - (ex - 1022);                       // |X| = mant 2^(11 - r)
+    unsigned long long X;
+    if (r <= 11) X = mant << (11 - r);
+    else if (r - 11 >= 64) X = 0;
+    else X = (mant + (1ull << (r - 12))) >> (r - 11);
+    xl = (uint32_t)X;
+    xh = (uint32_t)(X >> 32);
+    sgn = (uint32_t)((unsigned long long)bits >> 63);
 }
+
+// half2 of byte b (0 = lowest) of two fixed-point magnitudes, with their
+// signs: PRMT gathers the bytes, 0x6400 makes them 1024 + d in FP16, and one
+// HFMA2 applies +-1 and removes the 1024 (exact).
+__device__ __forceinline__ uint32_t digit_pair(int b, uint32_t al, uint32_t ah, uint32_t bl,
+                                               uint32_t bh, uint32_t smul, uint32_t sadd) {
+    const uint32_t wa = b >= 4 ? ah : al;
+    const uint32_t wb = b >= 4 ? bh : bl;
+    const uint32_t sel = (uint32_t)(b & 3) | ((uint32_t)(4 + (b & 3)) << 8);
+    uint32_t t;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(t) : "r"(wa), "r"(wb), "r"(sel));
+    t = (t & 0x00FF00FFu) | 0x64006400u;
+    __half2 h = *reinterpret_cast<__half2 *>(&t);
+    h = __hfma2(h, *reinterpret_cast<const __half2 *>(&smul), *reinterpret_cast<const __half2 *>(&sadd));
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
 
 template <int NT>
 __global__ void __launch_bounds__(kThreads, 1)
@@ -161,24 +206,26 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *A = smem;
     uint8_t *B = smem + G::A_BYTES;
-    uint64_t *bar = (uint64_t *)(B + G::B_BYTES);
-    uint32_t *tslot = (uint32_t *)(bar + 1);
-    double *red = (double *)(tslot + 4);   // 8 doubles, 8-byte aligned
-    int *rowmax = (int *)(red + 8);        // largest biased exponent of each tile row
+    uint8_t *aux = B + G::B_BYTES;
+    uint64_t *bars = (uint64_t *)aux;                 // 5 barriers
+    uint32_t *tslot = (uint32_t *)(aux + 64);
+    double *red = (double *)(aux + 128);              // 4 doubles
+    int *rowE = (int *)(aux + 1024);                  // producer -> MMA warp
+    int *rowE_epi = rowE + kM;                        // MMA warp -> epilogue
+    const uint32_t bA_full = saddr(&bars[0]), bA_empty = saddr(&bars[1]), bT_full = saddr(&bars[2]),
+                   bT_empty = saddr(&bars[3]), bX_full = saddr(&bars[4]);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int arr = blockIdx.z;
     const long long nlines = (long long)S.nL * S.nR;
-    const long long g0 = (long long)blockIdx.x * kM;
-    const int qc0 = S.qlo + blockIdx.y * kQC;
+    const long long nlb = (nlines + kM - 1) / kM;
+    const int nq = S.qhi - S.qlo + 1;
+    const int nch = (nq + kQC - 1) / kQC;
+    const long long ntiles = nlb * nch * S.narr;
     const int upfil = S.lowfil + NT - 1;
-    const int plast = S.qhi + upfil;            // last input index any output needs
-    const int kneed = kQC + NT - 1;             // positions the tile's outputs use
-    const double *__restrict__ x = S.x + (long long)arr * S.x_arr;
-    double *__restrict__ y = S.y + (long long)arr * S.y_arr;
-    const double *__restrict__ x2 = S.x2 ? S.x2 + (long long)arr * S.x_arr : nullptr;
+    const int plast = S.qhi + upfil;
+    const int kneed = kQC + NT - 1;
 
-    if (warp == 0) {
+    if (warp == 4) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
                          saddr(tslot)),
                      "r"(kTmemCols)
@@ -186,13 +233,16 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar)) : "memory");
+        bar_init(bA_full, 128);
+        bar_init(bA_empty, 1);
+        bar_init(bT_full, 1);
+        bar_init(bT_empty, 128);
+        bar_init(bX_full, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    for (int i = tid; i < kM; i += kThreads) rowmax[i] = 0;
-
-    // ---- Toeplitz filter tiles B_t[n][kk] = e_t(kk - n), K-major core matrices
-    for (int idx = tid; idx < kS * 16 * G::KB; idx += kThreads) {
+    if (tid < 4) red[tid] = 0.0;
+    // Toeplitz filter tiles B_t[n][kk] = e_t(kk - n), K-major core matrices
+    for (int idx = tid; idx < G::ND * 16 * G::KB; idx += kThreads) {
         const int t = idx / (16 * G::KB), rem = idx % (16 * G::KB);
         const int n = rem / G::KB, kk = rem % G::KB;
         const int tap = kk - n;
@@ -200,157 +250,279 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
         *(unsigned short *)(B + t * G::B_PLANE + (kk >> 3) * 256 + (n >> 3) * 128 + (n & 7) * 16 +
                             (kk & 7) * 2) = v;
     }
-    __syncthreads();
-
-    // ---- pass 1: largest exponent of each line segment (a thread always owns
-    // the same row: row = tid % 128)
-    constexpr int kChunks = G::KT / 8;
-    int mx = 0;
-    for (int id = tid; id < kM * kChunks; id += kThreads) {
-        const int row = id % kM, chunk = id / kM;
-        const long long g = g0 + row;
-        if (g >= nlines) continue;
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-            const int kk = chunk * 8 + e;
-            const int p = qc0 + S.lowfil + kk;
-            if (kk < kneed && p <= plast) {
-                const double v = fetch_conv(S, x, g, p);
-                const int ex = (int)((__double_as_longlong(v) >> 52) & 0x7FF);
-                mx = max(mx, ex);
-            }
-        }
-    }
-    atomicMax(&rowmax[tid % kM], mx);
-    __syncthreads();
-    const int E = (rowmax[tid % kM] ? rowmax[tid % kM] : 1) - 1022;   // |x| < 2^E on the row
-
-    // ---- pass 2: digit planes, 8 positions (one core-matrix row) per task
-    for (int id = tid; id < kM * kChunks; id += kThreads) {
-        const int row = id % kM, chunk = id / kM;
-        const long long g = g0 + row;
-        __half h[kS][8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-            const int kk = chunk * 8 + e;
-            const int p = qc0 + S.lowfil + kk;
-            double v = 0.0;
-            if (g < nlines && kk < kneed && p <= plast) v = fetch_conv(S, x, g, p);
-            int d[kS];
-            digits(v, E, d);
-#pragma unroll
-            for (int s = 0; s < kS; ++s) h[s][e] = __int2half_rn(d[s]);
-        }
-        const int off = chunk * 2048 + (row >> 3) * 128 + (row & 7) * 16;
-#pragma unroll
-        for (int s = 0; s < kS; ++s) {
-            uint4 v;
-            v.x = (uint32_t)__half_as_ushort(h[s][0]) | ((uint32_t)__half_as_ushort(h[s][1]) << 16);
-            v.y = (uint32_t)__half_as_ushort(h[s][2]) | ((uint32_t)__half_as_ushort(h[s][3]) << 16);
-            v.z = (uint32_t)__half_as_ushort(h[s][4]) | ((uint32_t)__half_as_ushort(h[s][5]) << 16);
-            v.w = (uint32_t)__half_as_ushort(h[s][6]) | ((uint32_t)__half_as_ushort(h[s][7]) << 16);
-            *(uint4 *)(A + s * G::A_PLANE + off) = v;
-        }
-    }
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = *tslot;
+    bool alive = true;
 
-    // ---- MMA issue: one thread; pairs are ordered by k, so the first pair of
-    // each order overwrites its accumulator and the others add to it
-    if (tid == 0) {
-        const uint32_t a0 = saddr(A), b0 = saddr(B);
-        for (int j = 0; j < kNB; ++j)
-            for (int i = 0; i < Pairs<NT>::N; ++i) {
-                const int k = pair_k(NT, i), s = pair_s(NT, i), t = k - s;
-                const bool first = i == 0 || pair_k(NT, i - 1) != k;
-                const uint32_t d = tmem + (uint32_t)((j * kG + k) * 16);
-                for (int ks = 0; ks < G::KB / 16; ++ks) {
-                    const uint64_t ad =
-                        umma_desc(a0 + s * G::A_PLANE + (2 * j + 2 * ks) * 2048, 2048, 128);
-                    const uint64_t bd = umma_desc(b0 + t * G::B_PLANE + 2 * ks * 256, 256, 128);
-                    mma_f16(d, ad, bd, (first && ks == 0) ? 0u : 1u);
+    if (warp < 4) {
+        // ================================ producers
+        uint32_t it = 0;
+        const long long *xbits = reinterpret_cast<const long long *>(S.x);
+        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+            if (it > 0 && !bar_wait(bA_empty, (it - 1) & 1)) { alive = false; break; }
+            const int ch = (int)(tile % nch);
+            const long long lb = (tile / nch) % nlb;
+            const int arr = (int)(tile / (nch * nlb));
+            const int p0 = S.qlo + ch * kQC + S.lowfil;
+            // periodic: start of the segment in [0, n); a segment wraps at most
+            // once when n >= KT, otherwise the slow modulo is used
+            const int pstart = S.bc == BC_PERIODIC ? imod(p0, S.n) : 0;
+            const bool onewrap = S.n >= G::KT;
+            auto pos_of = [&](int kk) -> int {       // array position, -1 for a zero
+                const int p = p0 + kk;
+                if (kk >= kneed || p > plast) return -1;
+                if (S.bc == BC_PERIODIC) {
+                    if (onewrap) { const int q = pstart + kk; return q >= S.n ? q - S.n : q; }
+                    return imod(p, S.n);
+                }
+                if (S.bc == BC_SHRINK) return p - S.in_lo;
+                return (p < 0 || p >= S.n) ? -1 : p;
+            };
+            if (S.nL == 1) {
+                // contiguous lines: one warp per row, lanes across positions
+                // (coalesced); 8 rows in flight per warp, values kept in registers
+                constexpr int J = (G::KT + 31) / 32;
+                constexpr int RB = 8;
+                for (int rb = 0; rb < 32; rb += RB) {
+                    long long bits[RB][J];
+#pragma unroll
+                    for (int i = 0; i < RB; ++i) {
+                        const long long g = lb * kM + warp * 32 + rb + i;
+                        const bool valid = g < nlines;
+                        const long long *base = xbits + (long long)arr * S.x_arr + (long long)S.in_ext * (valid ? g : 0);
+#pragma unroll
+                        for (int j = 0; j < J; ++j) {
+                            const int kk = lane + 32 * j;
+                            const int ps = (valid && kk < G::KT) ? pos_of(kk) : -1;
+                            bits[i][j] = ps >= 0 ? base[ps] : 0ll;
+                        }
+                    }
+#pragma unroll
+                    for (int i = 0; i < RB; ++i) {
+                        const int row = warp * 32 + rb + i;
+                        int mx = 0;
+#pragma unroll
+                        for (int j = 0; j < J; ++j) mx = max(mx, (int)((bits[i][j] >> 52) & 0x7FF));
+                        mx = __reduce_max_sync(0xffffffffu, mx);
+                        const int E = (mx ? mx : 1) - 1022;
+#pragma unroll
+                        for (int j = 0; j < J; ++j) {
+                            const int kk = lane + 32 * j;
+                            uint32_t xl, xh, sgn;
+                            fixed64(bits[i][j], E, xl, xh, sgn);
+                            // even lane packs (kk, kk+1) with its odd neighbour
+                            const uint32_t nl = __shfl_down_sync(0xffffffffu, xl, 1);
+                            const uint32_t nh = __shfl_down_sync(0xffffffffu, xh, 1);
+                            const uint32_t ns = __shfl_down_sync(0xffffffffu, sgn, 1);
+                            if ((lane & 1) == 0 && kk < G::KT) {
+                                const uint32_t smul = (0x3C00u | (sgn << 15)) | ((0x3C00u | (ns << 15)) << 16);
+                                const uint32_t sadd = (0xE400u ^ (sgn << 15)) | ((0xE400u ^ (ns << 15)) << 16);
+                                const int off = (kk >> 3) * 2048 + (row >> 3) * 128 + (row & 7) * 16 + (kk & 7) * 2;
+#pragma unroll
+                                for (int sd = 0; sd < G::ND; ++sd)
+                                    *(uint32_t *)(A + sd * G::A_PLANE + off) =
+                                        digit_pair(7 - sd, xl, xh, nl, nh, smul, sadd);
+                            }
+                        }
+                        if (lane == 0) rowE[row] = mx == 0x7FF ? 0x7FFFFFFF : E;
+                    }
+                }
+            } else {
+                // strided lines: half-warps over 16 consecutive lines (coalesced),
+                // lanes 0-15 hold positions [0, KT/2), lanes 16-31 [KT/2, KT)
+                constexpr int H = G::KT / 2;                      // multiple of 8
+                const int half = lane >> 4;
+                for (int rb = 0; rb < 32; rb += 16) {
+                    const int row = warp * 32 + rb + (lane & 15);
+                    const long long g = lb * kM + row;
+                    const bool valid = g < nlines;
+                    const long long l = valid ? g % S.nL : 0, r = valid ? g / S.nL : 0;
+                    const long long *base = xbits + (long long)arr * S.x_arr + l + (long long)S.nL * (long long)S.in_ext * r;
+                    const long long stride = S.nL;
+                    long long bits[H];
+#pragma unroll
+                    for (int e = 0; e < H; ++e) {
+                        const int ps = valid ? pos_of(half * H + e) : -1;
+                        bits[e] = ps >= 0 ? base[(long long)ps * stride] : 0ll;
+                    }
+                    int mx = 0;
+#pragma unroll
+                    for (int e = 0; e < H; ++e) mx = max(mx, (int)((bits[e] >> 52) & 0x7FF));
+                    mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
+                    const int E = (mx ? mx : 1) - 1022;
+#pragma unroll
+                    for (int c = 0; c < H / 8; ++c) {
+                        uint32_t xl[8], xh[8], sg[8];
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) fixed64(bits[c * 8 + e], E, xl[e], xh[e], sg[e]);
+                        const int off = (half * (H / 8) + c) * 2048 + (row >> 3) * 128 + (row & 7) * 16;
+#pragma unroll
+                        for (int sd = 0; sd < G::ND; ++sd) {
+                            uint32_t wds[4];
+#pragma unroll
+                            for (int w = 0; w < 4; ++w) {
+                                const uint32_t smul = (0x3C00u | (sg[2 * w] << 15)) |
+                                                      ((0x3C00u | (sg[2 * w + 1] << 15)) << 16);
+                                const uint32_t sadd = (0xE400u ^ (sg[2 * w] << 15)) |
+                                                      ((0xE400u ^ (sg[2 * w + 1] << 15)) << 16);
+                                wds[w] = digit_pair(7 - sd, xl[2 * w], xh[2 * w], xl[2 * w + 1], xh[2 * w + 1],
+                                                    smul, sadd);
+                            }
+                            *(uint4 *)(A + sd * G::A_PLANE + off) = make_uint4(wds[0], wds[1], wds[2], wds[3]);
+                        }
+                    }
+                    if (half == 0) rowE[row] = mx == 0x7FF ? 0x7FFFFFFF : E;
                 }
             }
-        asm volatile(
-            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                saddr(bar))
-            : "memory");
-    }
-
-    // ---- wait for the accumulators (bounded)
-    // give up after ~2 s of SM clock: report through *status, free TMEM, return
-    bool ok = false;
-    const long long t0 = clock64();
-    while (!(ok = mbar_try_wait(saddr(bar), 0)))
-        if (clock64() - t0 > 4000000000LL) break;
-    if (!ok && lane == 0) atomicExch(status, 1);
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-
-    // ---- epilogue: warp (w%4) owns TMEM lanes 32(w%4).., warps 0-3 / 4-7 split the blocks
-    const int lq = warp & 3, jb = warp >> 2;
-    const int row = lq * 32 + lane;
-    const long long g = g0 + row;
-    const long long l = g % S.nL, rr = g / S.nL;
-    const long long out_ext = S.out_ext;
-    const int rmax = rowmax[row];
-    const double scale = rmax == 0x7FF ? __longlong_as_double(0x7FF8000000000000LL)
-                                       : (S.has_a ? S.a : 1.0) * ldexp(1.0, (rmax ? rmax : 1) - 1022 + F.ef - 61);
-    double dot = 0.0;
-    for (int jj = 0; jj < kNB / 2; ++jj) {
-        const int j = jb * (kNB / 2) + jj;
-        uint32_t acc[kG][16];
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            bar_arrive(bA_full);
+        }
+    } else if (warp < 8) {
+        // ================================ epilogue
+        const int lq = warp - 4;
+        const int row = lq * 32 + lane;
+        double dot = 0.0;
+        uint32_t it = 0;
+        const uint32_t a0 = saddr(A), b0 = saddr(B);
+        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+            if (warp == 4) {
+                // ---- MMA issue for this tile: needs its A planes and the
+                // accumulators released by the epilogue of the previous tile
+                if (!bar_wait(bA_full, it & 1)) { alive = false; break; }
+                if (it > 0 && !bar_wait(bT_empty, (it - 1) & 1)) { alive = false; break; }
 #pragma unroll
-        for (int k = 0; k < kG; ++k)
-            tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)((j * kG + k) * 16), acc[k]);
-        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        if (!ok || g >= nlines) continue;
-#pragma unroll
-        for (int n = 0; n < 16; ++n) {
-            const int q = qc0 + 16 * j + n;
-            if (q > S.qhi) break;
-            long long Y = 0;
-#pragma unroll
-            for (int k = 0; k < 6; ++k)
-                Y += (long long)__float2int_rn(__uint_as_float(acc[k][n])) << (9 * (5 - k));
-            Y += ((long long)__float2int_rn(__uint_as_float(acc[6][n])) + 256) >> 9;
-            double out = __ll2double_rn(Y) * scale;
-            const long long pos = q - S.out_lo;
-            const long long yi = S.transpose ? rr + (long long)S.nR * pos
-                                             : l + (long long)S.nL * (pos + out_ext * rr);
-            if ((S.has_dot || S.has_ax) && (S.bc != BC_GROW || (q >= 0 && q < S.n))) {
-                const double xq = fetch_conv(S, x, g, q);
-                if (S.has_dot) dot = fma(xq, out, dot);
-                if (S.has_ax) out = fma(xq, S.a_x, out);
+                for (int i = 0; i < kM / 32; ++i) rowE_epi[lane + 32 * i] = rowE[lane + 32 * i];
+                __syncwarp();
+                if (lane == 0) {
+                    bar_arrive(bX_full);
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    for (int j = 0; j < kNB; ++j)
+                        for (int k = 0; k < G::ORD; ++k) {
+                            const int slo = k > 7 ? k - 7 : 0, shi = k < 7 ? k : 7;
+                            const uint32_t d = tmem + (uint32_t)((j * G::ORD + k) * 16);
+                            for (int s = slo; s <= shi; ++s) {
+                                const int t = k - s;
+                                for (int ks = 0; ks < G::KB / 16; ++ks) {
+                                    const uint64_t ad =
+                                        umma_desc(a0 + s * G::A_PLANE + (2 * j + 2 * ks) * 2048, 2048, 128);
+                                    const uint64_t bd =
+                                        umma_desc(b0 + t * G::B_PLANE + 2 * ks * 256, 256, 128);
+                                    mma_f16(d, ad, bd, (s == slo && ks == 0) ? 0u : 1u);
+                                }
+                            }
+                        }
+                    commit(bA_empty);
+                    commit(bT_full);
+                }
+                __syncwarp();
             }
-            if (x2) {
-                const long long x2i = S.bc == BC_GROW
-                    ? yi : l + (long long)S.nL * ((long long)(q - S.in_lo) + (long long)S.in_ext * rr);
-                out += x2[x2i];
+            if (!bar_wait(bX_full, it & 1) || !bar_wait(bT_full, it & 1)) { alive = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const int Er = rowE_epi[row];
+            const int ch = (int)(tile % nch);
+            const long long lb = (tile / nch) % nlb;
+            const int arr = (int)(tile / (nch * nlb));
+            const int qc0 = S.qlo + ch * kQC;
+            const long long g = lb * kM + row;
+            const bool valid = g < nlines;
+            const long long l = valid ? g % S.nL : 0, rr = valid ? g / S.nL : 0;
+            double *__restrict__ y = S.y + (long long)arr * S.y_arr;
+            const double *__restrict__ xa = S.x + (long long)arr * S.x_arr;
+            const double *__restrict__ x2 = S.x2 ? S.x2 + (long long)arr * S.x_arr : nullptr;
+            const int se = Er + F.ef - 56;
+            for (int j = 0; j < kNB; ++j) {
+                uint32_t acc[G::ORD][16];
+#pragma unroll
+                for (int k = 0; k < G::ORD; ++k)
+                    tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)((j * G::ORD + k) * 16),
+                              acc[k]);
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (!valid) continue;
+                const int q0 = qc0 + 16 * j;
+                const int nv = S.qhi - q0 + 1 < 16 ? S.qhi - q0 + 1 : 16;   // outputs in this block
+                if (nv <= 0) continue;
+                double add[16];
+                const bool full = nv == 16;
+#pragma unroll
+                for (int n = 0; n < 16; ++n) {
+                    add[n] = 0.0;
+                    const int q = q0 + n;
+                    if (x2 && (full || n < nv)) {
+                        const long long pos = q - S.out_lo;
+                        const long long x2i = S.bc == BC_GROW
+                            ? (S.transpose ? rr + (long long)S.nR * pos : l + (long long)S.nL * (pos + (long long)S.out_ext * rr))
+                            : l + (long long)S.nL * ((long long)(q - S.in_lo) + (long long)S.in_ext * rr);
+                        add[n] = x2[x2i];
+                    }
+                }
+#pragma unroll
+                for (int n = 0; n < 16; ++n) {
+                    if (!full && n >= nv) break;
+                    const int q = q0 + n;
+                    long long Y = 0;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k)
+                        Y += (long long)__float2int_rn(__uint_as_float(acc[k][n])) << (8 * (5 - k));
+                    Y += ((long long)__float2int_rn(__uint_as_float(acc[6][n])) + 128) >> 8;
+                    if (G::ORD > 7)
+                        Y += ((long long)__float2int_rn(__uint_as_float(acc[G::ORD - 1][n])) + 32768) >> 16;
+                    double out = Er == 0x7FFFFFFF ? __longlong_as_double(0x7FF8000000000000LL)
+                                                  : scaled_to_f64(Y, se);
+                    const long long pos = q - S.out_lo;
+                    const long long yi = S.transpose ? rr + (long long)S.nR * pos
+                                                     : l + (long long)S.nL * (pos + (long long)S.out_ext * rr);
+                    if ((S.has_dot || S.has_ax) && (S.bc != BC_GROW || (q >= 0 && q < S.n))) {
+                        const int ps = S.bc == BC_PERIODIC ? imod(q, S.n) : q - S.in_lo;
+                        const double xq = xa[l + (long long)S.nL * ((long long)ps + (long long)S.in_ext * rr)];
+                        if (S.has_dot) dot = fma(xq, out, dot);
+                        if (S.has_ax) out = fma(xq, S.a_x, out);
+                    }
+                    if (x2) out += add[n];
+                    if (S.ay_mode == 2) out += y[yi];
+                    else if (S.ay_mode == 1) out = fma(S.a_y, y[yi], out);
+                    y[yi] = out;
+                }
             }
-            if (S.ay_mode == 2) out += y[yi];
-            else if (S.ay_mode == 1) out = fma(S.a_y, y[yi], out);
-            y[yi] = out;
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            bar_arrive(bT_empty);
+        }
+        if (S.has_dot) {
+            for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+            if (lane == 0) red[lq] = dot;
         }
     }
-    if (S.has_dot) {
-        for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
-        if (lane == 0) red[warp] = dot;
-    }
+
+    if (!alive) atomicExch(status, 1);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
-    if (warp == 0)
+    if (warp == 4)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
                      "r"(kTmemCols)
                      : "memory");
-    if (S.has_dot && tid == 0) {
-        double s = 0.0;
-        for (int i = 0; i < kThreads / 32; ++i) s += red[i];
-        const long long b = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-        S.dot_part[b] = s;
+    if (S.has_dot && tid == 0) S.dot_part[blockIdx.x] = red[0] + red[1] + red[2] + red[3];
+}
+
+int g_sms[64] = {0};
+
+int sm_count() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 148;
+    if (!g_sms[dev]) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        g_sms[dev] = n > 0 ? n : 148;
     }
+    return g_sms[dev];
+}
+
+long long tile_count(const Sweep &S) {
+    const long long nlines = (long long)S.nL * S.nR;
+    const long long nq = S.qhi - S.qlo + 1;
+    return ((nlines + kM - 1) / kM) * ((nq + kQC - 1) / kQC) * S.narr;
 }
 
 template <int NT>
@@ -365,9 +537,8 @@ cudaError_t launch_t(const Sweep &S, const TcFilter &F, int *status, cudaStream_
         if (e != cudaSuccess) return e;
         if (dev >= 0 && dev < 64) attr[dev] = true;
     }
-    const long long nlines = (long long)S.nL * S.nR;
-    const int nq = S.qhi - S.qlo + 1;
-    dim3 grid((unsigned)((nlines + kM - 1) / kM), (unsigned)((nq + kQC - 1) / kQC), (unsigned)S.narr);
+    const long long tiles = tile_count(S);
+    const int grid = (int)(tiles < sm_count() ? tiles : sm_count());
     sweep_tc_kernel<NT><<<grid, kThreads, G::SMEM, st>>>(S, F, status);
     return cudaGetLastError();
 }
@@ -379,32 +550,48 @@ bool sweep_tc_supported(const Sweep &S) {
 }
 
 long long sweep_tc_blocks(const Sweep &S) {
-    const long long nlines = (long long)S.nL * S.nR;
-    const long long nq = S.qhi - S.qlo + 1;
-    return ((nlines + kM - 1) / kM) * ((nq + kQC - 1) / kQC) * S.narr;
+    const long long tiles = tile_count(S);
+    return tiles < sm_count() ? tiles : sm_count();
 }
 
-void tc_filter_digits(const double *taps, int ntaps, TcFilter &F) {
-    double m = 0.0;
-    for (int i = 0; i < ntaps; ++i) m = fmax(m, fabs(taps[i]));
-    int ef = 0;
-    frexp(m, &ef);                       // m < 2^ef
+// Filter bytes with the operator scalar folded in exactly: a*f is formed as
+// the 106-bit product of the two mantissas, then rounded once to the 64-bit
+// fixed point |a f| 2^(64 - ef) (ef: power of two above the largest |a f|).
+void tc_filter_digits(const double *taps, int ntaps, double a, TcFilter &F) {
+    int ea = 0;
+    const double fa = frexp(fabs(a), &ea);                          // |a| = fa 2^ea
+    const unsigned long long ma = (unsigned long long)ldexp(fa, 53);  // 53-bit integer
+    unsigned __int128 prod[TcFilter::kMaxTaps];
+    int ep[TcFilter::kMaxTaps];
+    int ef = -100000;
+    for (int i = 0; i < ntaps; ++i) {
+        int e = 0;
+        const double ff = frexp(fabs(taps[i]), &e);
+        const unsigned long long mf = (unsigned long long)ldexp(ff, 53);
+        prod[i] = (unsigned __int128)ma * mf;
+        ep[i] = (ea - 53) + (e - 53);                               // |a f| = prod 2^ep
+        if (prod[i]) {
+            int bl = 0;
+            for (unsigned __int128 t = prod[i]; t; t >>= 1) ++bl;
+            if (bl + ep[i] > ef) ef = bl + ep[i];                   // |a f| < 2^(bl + ep)
+        }
+    }
+    if (ef == -100000) ef = 0;
     F.ef = ef;
     for (int s = 0; s < TcFilter::kSlices; ++s)
         for (int i = 0; i < TcFilter::kMaxTaps; ++i) F.dig[s][i] = 0;
     for (int i = 0; i < ntaps; ++i) {
-        const double v = taps[i];
-        long long X = llround(ldexp(fabs(v), 62 - ef));   // exact: 53-bit taps shifted up
-        if (v < 0) X = -X;
-        int d[TcFilter::kSlices];
-        for (int s = TcFilter::kSlices - 1; s >= 1; --s) {
-            const long long u = X + 256;
-            d[s] = (int)(u & 511) - 256;
-            X = u >> 9;
+        const int sh = ep[i] + 64 - ef;                             // |F| = prod 2^sh < 2^64
+        const unsigned __int128 v = prod[i];
+        unsigned long long X;
+        if (sh >= 0) X = (unsigned long long)(v << sh);
+        else if (-sh >= 127) X = 0;
+        else X = (unsigned long long)((v + ((unsigned __int128)1 << (-sh - 1))) >> (-sh));
+        const bool neg = (a < 0) != (taps[i] < 0);
+        for (int s = 0; s < TcFilter::kSlices; ++s) {
+            const int byte = (int)((X >> (8 * (7 - s))) & 0xFF);
+            F.dig[s][i] = __half_as_ushort(__int2half_rn(neg ? -byte : byte));
         }
-        d[0] = (int)X;
-        for (int s = 0; s < TcFilter::kSlices; ++s)
-            F.dig[s][i] = __half_as_ushort(__int2half_rn(d[s]));
     }
 }
 

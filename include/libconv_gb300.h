@@ -151,6 +151,11 @@ int d_rfsf_ld_narr(int d, const int *n, const int *bc, const int *nx, const int 
  * Periodic and free (no-grow) boundaries. */
 int d_kin(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
           double *w2, const double *a, double a_x, double a_y);
+/* Extension (no counterpart in the generated code, which has no narr for
+ * Kinetic()): the same 3D kinetic over narr grids laid back to back in x, y,
+ * w1 and w2, in one launch per sweep. */
+int d_kin_narr(int d, const int *n, const int *bc, int narr, const double *x, double *y,
+               double *w1, double *w2, const double *a, double a_x, double a_y);
 /* 3D wavelet analysis / synthesis (transpose = 1, work): Wavelet() of
  * BigDFT/Wavelet2.rb:2-21 (BigDFT/Wavelet_test2.rb:86-154). */
 int d_dwt_sym8(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
@@ -168,6 +173,8 @@ int d_rfsf_ld_narr_dev(int d, const int *n, const int *bc, const int *nx, const 
                        void *stream);
 int d_kin_dev(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
               double *w2, const double *a, double a_x, double a_y, void *stream);
+int d_kin_narr_dev(int d, const int *n, const int *bc, int narr, const double *x, double *y,
+                   double *w1, double *w2, const double *a, double a_x, double a_y, void *stream);
 int d_dwt_sym8_dev(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
                    double *w2, void *stream);
 int d_idwt_sym8_dev(int d, const int *n, const int *bc, const double *x, double *y,

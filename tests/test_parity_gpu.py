@@ -287,3 +287,21 @@ def test_full_size_wavelet_round_trip_96(pkg, O):
     assert rel(r, ro) <= TOL
     pkg.Kernel('d_dwt_sym8').run(3, n, [0, 0, 0], r, back, w, w)
     assert np.abs(back - s).max() < 1e-11
+
+
+def test_kinetic3d_narr_extension(pkg, O):
+    """d_kin_narr: the 3D kinetic over narr grids in one call equals d_kin on each."""
+    n = [10, 17, 12]
+    N = int(np.prod(n))
+    narr = 3
+    x = seeded(30, N * narr)
+    a = [-0.5 / 0.45 ** 2] * 3
+    y0 = seeded(31, N * narr)
+    yg = y0.copy()
+    w = np.zeros(1)
+    pkg.Kernel('d_kin_narr').run(3, n, [0, 0, 0], narr, x, yg, w, w, a, 0.25, 0.5)
+    for j in range(narr):
+        yo = y0[j * N:(j + 1) * N].copy()
+        assert O.call('oracle_d_kin', 3, n, [0, 0, 0], x[j * N:(j + 1) * N].copy(), yo,
+                      np.zeros(N), np.zeros(N), np.array(a), 0.25, 0.5) == 0
+        assert rel(yg[j * N:(j + 1) * N], yo) <= TOL
