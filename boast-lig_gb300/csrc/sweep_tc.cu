@@ -25,18 +25,18 @@
 // with K = 32 (16 taps) or 48 (29 taps); A is a digit plane of the tile,
 // addressed at an offset of 16 positions per output block.
 //
-// Persistent, warp-specialised CTA (one per SM), single A buffer and single
-// TMEM accumulator set, 256 threads:
-//   warps 0-3  producers: largest exponent of each row segment, then its
-//              byte digits into the A planes (contiguous lines: one warp per
-//              row, lanes across positions; strided lines: one thread per row,
-//              lanes across consecutive lines; both coalesced);
-//   warps 4-7  epilogue: thread = TMEM lane = tile row; TMEM -> FP64 -> global;
-//              warp 4 also allocates TMEM and, once the epilogue has released
-//              the accumulators of tile i, issues the MMAs of tile i+1 (lane 0).
-// Producers fill tile i+1 while the epilogue drains tile i.  Every hand-off is
-// an mbarrier whose phase can never run two phases ahead of its waiter, and
-// every wait gives up after ~2 s of SM clock (status word set, TMEM freed).
+// Persistent, warp-specialised CTA (one per SM), 256 threads, one A buffer and
+// two TMEM accumulator halves (blocks 0-1 and 2-3 of a tile, 256 columns each):
+//   warps 0-3  producers: thread = (row, half of the row segment): largest
+//              exponent of the row, then its byte digits into the A planes
+//              (coalesced or vector loads); warp 0 then issues the tile's MMAs
+//              (lane 0, fully unrolled, precomputed descriptors), each TMEM
+//              half as soon as the epilogue has released it;
+//   warps 4-7  epilogue: thread = TMEM lane = tile row; TMEM -> FP64 -> global.
+// Producers fill tile i+1 while the epilogue drains tile i, and the MMAs of a
+// TMEM half overlap the draining of the other.  Every hand-off is an mbarrier
+// whose phase can never run two phases ahead of its waiter, and every wait
+// gives up after ~2 s of SM clock (status word set, TMEM freed).
 #include <cuda_fp16.h>
 #include <stdint.h>
 
@@ -62,9 +62,10 @@ template <int NT> struct TcGeom {
     static constexpr int B_PLANE = 16 * KB * 2;
     static constexpr int A_BYTES = ND * A_PLANE;
     static constexpr int B_BYTES = ND * B_PLANE;
-    static constexpr int AUX = 1024 + 2 * 4 * kM;               // barriers, slots, row exponents
+    static constexpr int AUX = 1024 + 3 * 4 * kM;               // barriers, slots, row exponents
     static constexpr int SMEM = A_BYTES + B_BYTES + AUX + 1024;
-    static_assert(ORD * kNB * 16 <= (int)kTmemCols, "TMEM columns");
+    static constexpr int HALF_COLS = 2 * ORD * 16;             // one TMEM half (2 blocks)
+    static_assert(2 * HALF_COLS <= (int)kTmemCols && HALF_COLS <= 256, "TMEM columns");
 };
 
 // ---- PTX wrappers ----------------------------------------------------------------
@@ -143,8 +144,6 @@ __device__ __forceinline__ int imod(int a, int n) {
     return r < 0 ? r + n : r;
 }
 
-__device__ __noinline__ double scaled_slow(long long Y, int se) { return ldexp((double)Y, se); }
-
 // int64 Y times 2^se as an FP64, rounded to nearest even, built from the bits.
 __device__ __forceinline__ double scaled_to_f64(long long Y, int se) {
     if (Y == 0) return 0.0;
@@ -157,28 +156,41 @@ __device__ __forceinline__ double scaled_to_f64(long long Y, int se) {
     mant += (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
     int e = 63 - lz + se;
     if (mant >> 53) { mant >>= 1; ++e; }
-    if (e < -1022 || e > 1023) return scaled_slow(Y, se);    // outside the normal range
+    if (e > 1023) return __longlong_as_double((long long)(neg | 0x7FF0000000000000ull));   // overflow
+    if (e < -1022) {                                   // subnormal (re-rounded) or zero
+        const int sh = -1022 - e;
+        mant = sh >= 54 ? 0ull : (mant + ((1ull << sh) >> 1)) >> sh;
+        return __longlong_as_double((long long)(neg | mant));
+    }
     return __longlong_as_double((long long)(neg | ((unsigned long long)(e + 1023) << 52) |
                                             (mant & 0xFFFFFFFFFFFFFull)));
 }
 
 
 // Fixed-point magnitude |X| = round(|x| 2^(64-E)) of the FP64 bit pattern
-// (|x| < 2^E), split in 32-bit words, and the sign bit.  Integer only.
+// (|x| < 2^E), split in 32-bit words, and the sign bit.  Integer only:
+// left shifts (values within 2^11 of the row maximum) are two funnel shifts.
 __device__ __forceinline__ void fixed64(long long bits, int E, uint32_t &xl, uint32_t &xh,
                                         uint32_t &sgn) {
-    int ex = (int)((bits >> 52) & 0x7FF);
-    unsigned long long mant = (unsigned long long)bits & 0xFFFFFFFFFFFFFull;
-    if (ex) mant |= 1ull << 52;
+    const uint32_t lo = (uint32_t)bits, hi = (uint32_t)((unsigned long long)bits >> 32);
+    int ex = (int)((hi >> 20) & 0x7FF);
+    uint32_t mh = hi & 0xFFFFFu;
+    if (ex) mh |= 0x100000u;
     else ex = 1;
+    sgn = hi >> 31;
     const int r = E - (ex - 1022);                       // |X| = mant 2^(11 - r)
-    unsigned long long X;
-    if (r <= 11) X = mant << (11 - r);
-    else if (r - 11 >= 64) X = 0;
-    else X = (mant + (1ull << (r - 12))) >> (r - 11);
-    xl = (uint32_t)X;
-    xh = (uint32_t)(X >> 32);
-    sgn = (uint32_t)((unsigned long long)bits >> 63);
+    if (r <= 11) {
+        const uint32_t c = (uint32_t)(11 - r);           // 0..11
+        xh = __funnelshift_l(lo, mh, c);
+        xl = lo << c;
+    } else {
+        const int c = r - 11;                            // right shift with rounding
+        if (c >= 64) { xl = xh = 0; return; }
+        unsigned long long m = ((unsigned long long)mh << 32) | lo;
+        m = (m + (1ull << (c - 1))) >> c;
+        xl = (uint32_t)m;
+        xh = (uint32_t)(m >> 32);
+    }
 }
 
 // half2 of byte b (0 = lowest) of two fixed-point magnitudes, with their
@@ -198,6 +210,32 @@ __device__ __forceinline__ uint32_t digit_pair(int b, uint32_t al, uint32_t ah, 
 }
 
 
+// Issue the MMAs of one TMEM half (output blocks 2h, 2h+1) of a tile.  Orders
+// k = s + t are accumulated one per 16-column accumulator; the first pair of
+// an order overwrites it.  Descriptors are advanced by adding the (16-byte
+// unit) offset to the start-address field (addresses < 256 KB never carry).
+template <int NT, int H>
+__device__ __forceinline__ void issue_half(uint32_t tmem, uint64_t a_desc0, uint64_t b_desc0) {
+    using G = TcGeom<NT>;
+#pragma unroll
+    for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+        for (int k = 0; k < G::ORD; ++k) {
+            const uint32_t d = tmem + (uint32_t)(H * G::HALF_COLS + (jj * G::ORD + k) * 16);
+            constexpr int dummy = 0;
+            (void)dummy;
+#pragma unroll
+            for (int s = (k > 7 ? k - 7 : 0); s <= (k < 7 ? k : 7); ++s)
+#pragma unroll
+                for (int ks = 0; ks < G::KB / 16; ++ks) {
+                    const int j = 2 * H + jj;
+                    const uint64_t ad = a_desc0 + (uint64_t)((s * G::A_PLANE + (2 * j + 2 * ks) * 2048) >> 4);
+                    const uint64_t bd = b_desc0 + (uint64_t)(((k - s) * G::B_PLANE + 2 * ks * 256) >> 4);
+                    mma_f16(d, ad, bd, (s == (k > 7 ? k - 7 : 0) && ks == 0) ? 0u : 1u);
+                }
+        }
+}
+
 template <int NT>
 __global__ void __launch_bounds__(kThreads, 1)
 sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
@@ -207,13 +245,15 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
     uint8_t *A = smem;
     uint8_t *B = smem + G::A_BYTES;
     uint8_t *aux = B + G::B_BYTES;
-    uint64_t *bars = (uint64_t *)aux;                 // 5 barriers
+    uint64_t *bars = (uint64_t *)aux;                 // 7 barriers
     uint32_t *tslot = (uint32_t *)(aux + 64);
     double *red = (double *)(aux + 128);              // 4 doubles
-    int *rowE = (int *)(aux + 1024);                  // producer -> MMA warp
-    int *rowE_epi = rowE + kM;                        // MMA warp -> epilogue
-    const uint32_t bA_full = saddr(&bars[0]), bA_empty = saddr(&bars[1]), bT_full = saddr(&bars[2]),
-                   bT_empty = saddr(&bars[3]), bX_full = saddr(&bars[4]);
+    int *rowE = (int *)(aux + 1024);                  // producers -> MMA issuer
+    int *rowE_epi = rowE + kM;                        // MMA issuer -> epilogue, by tile parity
+    const uint32_t bA_full = saddr(&bars[0]), bA_empty = saddr(&bars[1]),
+                   bT_full0 = saddr(&bars[2]), bT_full1 = saddr(&bars[3]),
+                   bT_empty0 = saddr(&bars[4]), bT_empty1 = saddr(&bars[5]),
+                   bX_full = saddr(&bars[6]);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const long long nlines = (long long)S.nL * S.nR;
@@ -225,7 +265,7 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
     const int plast = S.qhi + upfil;
     const int kneed = kQC + NT - 1;
 
-    if (warp == 4) {
+    if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
                          saddr(tslot)),
                      "r"(kTmemCols)
@@ -235,8 +275,10 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
     if (tid == 0) {
         bar_init(bA_full, 128);
         bar_init(bA_empty, 1);
-        bar_init(bT_full, 1);
-        bar_init(bT_empty, 128);
+        bar_init(bT_full0, 1);
+        bar_init(bT_full1, 1);
+        bar_init(bT_empty0, 128);
+        bar_init(bT_empty1, 128);
         bar_init(bX_full, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
@@ -257,8 +299,10 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
     const uint32_t tmem = *tslot;
     bool alive = true;
 
+    const uint64_t a_desc0 = umma_desc(saddr(A), 2048, 128);
+    const uint64_t b_desc0 = umma_desc(saddr(B), 256, 128);
     if (warp < 4) {
-        // ================================ producers
+        // ================================ producers (+ MMA issue in warp 0)
         uint32_t it = 0;
         const long long *xbits = reinterpret_cast<const long long *>(S.x);
         for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
@@ -281,104 +325,103 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
                 if (S.bc == BC_SHRINK) return p - S.in_lo;
                 return (p < 0 || p >= S.n) ? -1 : p;
             };
-            if (S.nL == 1) {
-                // contiguous lines: one warp per row, lanes across positions
-                // (coalesced); 8 rows in flight per warp, values kept in registers
-                constexpr int J = (G::KT + 31) / 32;
-                constexpr int RB = 8;
-                for (int rb = 0; rb < 32; rb += RB) {
-                    long long bits[RB][J];
+            // thread = (row, half of the row segment): half-warps cover 16 rows,
+            // lanes 0-15 hold positions [0, KT/2), lanes 16-31 [KT/2, KT)
+            constexpr int H = G::KT / 2;                          // multiple of 8
+            const int half = lane >> 4;
+            for (int rb = 0; rb < 32; rb += 16) {
+                const int row = warp * 32 + rb + (lane & 15);
+                const long long g = lb * kM + row;
+                const bool valid = g < nlines;
+                const long long l = valid ? g % S.nL : 0, r = valid ? g / S.nL : 0;
+                const long long *base = xbits + (long long)arr * S.x_arr + l + (long long)S.nL * (long long)S.in_ext * r;
+                const long long stride = S.nL;
+                long long bits[H];
+                // contiguous fast path: the needed part of the half segment,
+                // [k0, k0 + len), is one unbroken, 16-byte aligned run of array
+                // positions -> vector loads (+ one scalar tail); zeros beyond
+                const int k0 = half * H;
+                const int klim = min(kneed, plast - p0 + 1);       // positions any output needs
+                const int len = max(0, min(H, klim - k0));
+                const int ps0 = len > 0 ? pos_of(k0) : -1;
+                const int psl = len > 0 ? pos_of(k0 + len - 1) : -1;
+                const bool run = valid && stride == 1 && ps0 >= 0 && psl == ps0 + len - 1 &&
+                                 ((((uintptr_t)(base + ps0)) & 15) == 0);
+                if (run) {
+                    const double2 *v = reinterpret_cast<const double2 *>(base + ps0);
 #pragma unroll
-                    for (int i = 0; i < RB; ++i) {
-                        const long long g = lb * kM + warp * 32 + rb + i;
-                        const bool valid = g < nlines;
-                        const long long *base = xbits + (long long)arr * S.x_arr + (long long)S.in_ext * (valid ? g : 0);
-#pragma unroll
-                        for (int j = 0; j < J; ++j) {
-                            const int kk = lane + 32 * j;
-                            const int ps = (valid && kk < G::KT) ? pos_of(kk) : -1;
-                            bits[i][j] = ps >= 0 ? base[ps] : 0ll;
+                    for (int e = 0; e < H / 2; ++e) {
+                        if (2 * e + 1 < len) {
+                            const double2 t = v[e];
+                            bits[2 * e] = __double_as_longlong(t.x);
+                            bits[2 * e + 1] = __double_as_longlong(t.y);
+                        } else {
+                            bits[2 * e] = 2 * e < len ? base[ps0 + 2 * e] : 0ll;
+                            bits[2 * e + 1] = 0ll;
                         }
                     }
-#pragma unroll
-                    for (int i = 0; i < RB; ++i) {
-                        const int row = warp * 32 + rb + i;
-                        int mx = 0;
-#pragma unroll
-                        for (int j = 0; j < J; ++j) mx = max(mx, (int)((bits[i][j] >> 52) & 0x7FF));
-                        mx = __reduce_max_sync(0xffffffffu, mx);
-                        const int E = (mx ? mx : 1) - 1022;
-#pragma unroll
-                        for (int j = 0; j < J; ++j) {
-                            const int kk = lane + 32 * j;
-                            uint32_t xl, xh, sgn;
-                            fixed64(bits[i][j], E, xl, xh, sgn);
-                            // even lane packs (kk, kk+1) with its odd neighbour
-                            const uint32_t nl = __shfl_down_sync(0xffffffffu, xl, 1);
-                            const uint32_t nh = __shfl_down_sync(0xffffffffu, xh, 1);
-                            const uint32_t ns = __shfl_down_sync(0xffffffffu, sgn, 1);
-                            if ((lane & 1) == 0 && kk < G::KT) {
-                                const uint32_t smul = (0x3C00u | (sgn << 15)) | ((0x3C00u | (ns << 15)) << 16);
-                                const uint32_t sadd = (0xE400u ^ (sgn << 15)) | ((0xE400u ^ (ns << 15)) << 16);
-                                const int off = (kk >> 3) * 2048 + (row >> 3) * 128 + (row & 7) * 16 + (kk & 7) * 2;
-#pragma unroll
-                                for (int sd = 0; sd < G::ND; ++sd)
-                                    *(uint32_t *)(A + sd * G::A_PLANE + off) =
-                                        digit_pair(7 - sd, xl, xh, nl, nh, smul, sadd);
-                            }
-                        }
-                        if (lane == 0) rowE[row] = mx == 0x7FF ? 0x7FFFFFFF : E;
-                    }
-                }
-            } else {
-                // strided lines: half-warps over 16 consecutive lines (coalesced),
-                // lanes 0-15 hold positions [0, KT/2), lanes 16-31 [KT/2, KT)
-                constexpr int H = G::KT / 2;                      // multiple of 8
-                const int half = lane >> 4;
-                for (int rb = 0; rb < 32; rb += 16) {
-                    const int row = warp * 32 + rb + (lane & 15);
-                    const long long g = lb * kM + row;
-                    const bool valid = g < nlines;
-                    const long long l = valid ? g % S.nL : 0, r = valid ? g / S.nL : 0;
-                    const long long *base = xbits + (long long)arr * S.x_arr + l + (long long)S.nL * (long long)S.in_ext * r;
-                    const long long stride = S.nL;
-                    long long bits[H];
+                } else {
 #pragma unroll
                     for (int e = 0; e < H; ++e) {
-                        const int ps = valid ? pos_of(half * H + e) : -1;
+                        const int ps = valid ? pos_of(k0 + e) : -1;
                         bits[e] = ps >= 0 ? base[(long long)ps * stride] : 0ll;
                     }
-                    int mx = 0;
-#pragma unroll
-                    for (int e = 0; e < H; ++e) mx = max(mx, (int)((bits[e] >> 52) & 0x7FF));
-                    mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
-                    const int E = (mx ? mx : 1) - 1022;
-#pragma unroll
-                    for (int c = 0; c < H / 8; ++c) {
-                        uint32_t xl[8], xh[8], sg[8];
-#pragma unroll
-                        for (int e = 0; e < 8; ++e) fixed64(bits[c * 8 + e], E, xl[e], xh[e], sg[e]);
-                        const int off = (half * (H / 8) + c) * 2048 + (row >> 3) * 128 + (row & 7) * 16;
-#pragma unroll
-                        for (int sd = 0; sd < G::ND; ++sd) {
-                            uint32_t wds[4];
-#pragma unroll
-                            for (int w = 0; w < 4; ++w) {
-                                const uint32_t smul = (0x3C00u | (sg[2 * w] << 15)) |
-                                                      ((0x3C00u | (sg[2 * w + 1] << 15)) << 16);
-                                const uint32_t sadd = (0xE400u ^ (sg[2 * w] << 15)) |
-                                                      ((0xE400u ^ (sg[2 * w + 1] << 15)) << 16);
-                                wds[w] = digit_pair(7 - sd, xl[2 * w], xh[2 * w], xl[2 * w + 1], xh[2 * w + 1],
-                                                    smul, sadd);
-                            }
-                            *(uint4 *)(A + sd * G::A_PLANE + off) = make_uint4(wds[0], wds[1], wds[2], wds[3]);
-                        }
-                    }
-                    if (half == 0) rowE[row] = mx == 0x7FF ? 0x7FFFFFFF : E;
                 }
+                int mx = 0;
+#pragma unroll
+                for (int e = 0; e < H; ++e) mx = max(mx, (int)(((unsigned long long)bits[e] >> 52) & 0x7FF));
+                mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
+                const int E = (mx ? mx : 1) - 1022;
+#pragma unroll
+                for (int c = 0; c < H / 8; ++c) {
+                    uint32_t xl[8], xh[8], sg[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) fixed64(bits[c * 8 + e], E, xl[e], xh[e], sg[e]);
+                    uint32_t smul[4], sadd[4];
+#pragma unroll
+                    for (int w = 0; w < 4; ++w) {
+                        smul[w] = (0x3C00u | (sg[2 * w] << 15)) | ((0x3C00u | (sg[2 * w + 1] << 15)) << 16);
+                        sadd[w] = (0xE400u ^ (sg[2 * w] << 15)) | ((0xE400u ^ (sg[2 * w + 1] << 15)) << 16);
+                    }
+                    const int off = (half * (H / 8) + c) * 2048 + (row >> 3) * 128 + (row & 7) * 16;
+#pragma unroll
+                    for (int sd = 0; sd < G::ND; ++sd) {
+                        uint32_t wds[4];
+#pragma unroll
+                        for (int w = 0; w < 4; ++w)
+                            wds[w] = digit_pair(7 - sd, xl[2 * w], xh[2 * w], xl[2 * w + 1], xh[2 * w + 1],
+                                                smul[w], sadd[w]);
+                        *(uint4 *)(A + sd * G::A_PLANE + off) = make_uint4(wds[0], wds[1], wds[2], wds[3]);
+                    }
+                }
+                if (half == 0) rowE[row] = mx == 0x7FF ? 0x7FFFFFFF : E;
             }
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             bar_arrive(bA_full);
+            if (warp == 0) {
+                // ---- MMA issue for this tile, one TMEM half at a time
+                if (!bar_wait(bA_full, it & 1)) { alive = false; break; }
+                if (it > 0 && !bar_wait(bT_empty0, (it - 1) & 1)) { alive = false; break; }
+#pragma unroll
+                for (int i = 0; i < kM / 32; ++i)
+                    rowE_epi[(it & 1) * kM + lane + 32 * i] = rowE[lane + 32 * i];
+                __syncwarp();
+                if (lane == 0) {
+                    bar_arrive(bX_full);
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    issue_half<NT, 0>(tmem, a_desc0, b_desc0);
+                    commit(bT_full0);
+                }
+                __syncwarp();
+                if (it > 0 && !bar_wait(bT_empty1, (it - 1) & 1)) { alive = false; break; }
+                if (lane == 0) {
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    issue_half<NT, 1>(tmem, a_desc0, b_desc0);
+                    commit(bT_full1);
+                    commit(bA_empty);
+                }
+                __syncwarp();
+            }
         }
     } else if (warp < 8) {
         // ================================ epilogue
@@ -386,42 +429,9 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
         const int row = lq * 32 + lane;
         double dot = 0.0;
         uint32_t it = 0;
-        const uint32_t a0 = saddr(A), b0 = saddr(B);
         for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
-            if (warp == 4) {
-                // ---- MMA issue for this tile: needs its A planes and the
-                // accumulators released by the epilogue of the previous tile
-                if (!bar_wait(bA_full, it & 1)) { alive = false; break; }
-                if (it > 0 && !bar_wait(bT_empty, (it - 1) & 1)) { alive = false; break; }
-#pragma unroll
-                for (int i = 0; i < kM / 32; ++i) rowE_epi[lane + 32 * i] = rowE[lane + 32 * i];
-                __syncwarp();
-                if (lane == 0) {
-                    bar_arrive(bX_full);
-                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                    for (int j = 0; j < kNB; ++j)
-                        for (int k = 0; k < G::ORD; ++k) {
-                            const int slo = k > 7 ? k - 7 : 0, shi = k < 7 ? k : 7;
-                            const uint32_t d = tmem + (uint32_t)((j * G::ORD + k) * 16);
-                            for (int s = slo; s <= shi; ++s) {
-                                const int t = k - s;
-                                for (int ks = 0; ks < G::KB / 16; ++ks) {
-                                    const uint64_t ad =
-                                        umma_desc(a0 + s * G::A_PLANE + (2 * j + 2 * ks) * 2048, 2048, 128);
-                                    const uint64_t bd =
-                                        umma_desc(b0 + t * G::B_PLANE + 2 * ks * 256, 256, 128);
-                                    mma_f16(d, ad, bd, (s == slo && ks == 0) ? 0u : 1u);
-                                }
-                            }
-                        }
-                    commit(bA_empty);
-                    commit(bT_full);
-                }
-                __syncwarp();
-            }
-            if (!bar_wait(bX_full, it & 1) || !bar_wait(bT_full, it & 1)) { alive = false; break; }
-            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const int Er = rowE_epi[row];
+            if (!bar_wait(bX_full, it & 1)) { alive = false; break; }
+            const int Er = rowE_epi[(it & 1) * kM + row];
             const int ch = (int)(tile % nch);
             const long long lb = (tile / nch) % nlb;
             const int arr = (int)(tile / (nch * nlb));
@@ -434,12 +444,21 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
             const double *__restrict__ x2 = S.x2 ? S.x2 + (long long)arr * S.x_arr : nullptr;
             const int se = Er + F.ef - 56;
             for (int j = 0; j < kNB; ++j) {
+                if ((j & 1) == 0) {                 // entering TMEM half j/2
+                    if (!bar_wait(j ? bT_full1 : bT_full0, it & 1)) { alive = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                }
                 uint32_t acc[G::ORD][16];
 #pragma unroll
                 for (int k = 0; k < G::ORD; ++k)
-                    tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)((j * G::ORD + k) * 16),
+                    tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) +
+                                  (uint32_t)((j >> 1) * G::HALF_COLS + ((j & 1) * G::ORD + k) * 16),
                               acc[k]);
                 asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (j & 1) {                        // half drained: release it
+                    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+                    bar_arrive(j == 1 ? bT_empty0 : bT_empty1);
+                }
                 if (!valid) continue;
                 const int q0 = qc0 + 16 * j;
                 const int nv = S.qhi - q0 + 1 < 16 ? S.qhi - q0 + 1 : 16;   // outputs in this block
@@ -486,8 +505,7 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
                     y[yi] = out;
                 }
             }
-            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-            bar_arrive(bT_empty);
+            if (!alive) break;
         }
         if (S.has_dot) {
             for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
@@ -498,7 +516,7 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
     if (!alive) atomicExch(status, 1);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
-    if (warp == 4)
+    if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
                      "r"(kTmemCols)
                      : "memory");
