@@ -25,14 +25,16 @@
 // with K = 32 (16 taps) or 48 (29 taps); A is a digit plane of the tile,
 // addressed at an offset of 16 positions per output block.
 //
-// Persistent, warp-specialised CTA (one per SM), 256 threads, one A buffer and
-// two TMEM accumulator halves (blocks 0-1 and 2-3 of a tile, 256 columns each):
-//   warps 0-3  producers: thread = (row, half of the row segment): largest
+// Persistent, warp-specialised CTA (one per SM), 512 threads at <= 128
+// registers, one A buffer and two TMEM accumulator halves (blocks 0-1 and 2-3
+// of a tile, 256 columns each):
+//   warps 0-7  producers: thread = (row, half of the row segment): largest
 //              exponent of the row, then its byte digits into the A planes
 //              (coalesced or vector loads); warp 0 then issues the tile's MMAs
 //              (lane 0, fully unrolled, precomputed descriptors), each TMEM
 //              half as soon as the epilogue has released it;
-//   warps 4-7  epilogue: thread = TMEM lane = tile row; TMEM -> FP64 -> global.
+//   warps 8-15 epilogue: warps 8-11 drain TMEM half 0, warps 12-15 half 1;
+//              thread = TMEM lane = tile row; TMEM -> FP64 -> global.
 // Producers fill tile i+1 while the epilogue drains tile i, and the MMAs of a
 // TMEM half overlap the draining of the other.  Every hand-off is an mbarrier
 // whose phase can never run two phases ahead of its waiter, and every wait
@@ -49,7 +51,8 @@ namespace {
 constexpr int kM = 128;          // lines per tile (MMA M)
 constexpr int kQC = 64;          // outputs per tile
 constexpr int kNB = kQC / 16;    // 16-output blocks per tile
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;     // 8 producer warps + 8 epilogue warps
+constexpr int kProducers = 256;
 constexpr uint32_t kTmemCols = 512;
 constexpr long long kWaitCycles = 4000000000LL;
 
@@ -128,15 +131,12 @@ __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
     return true;
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-        "%14,%15}, [%16];\n"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-          "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr)
-        : "memory");
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                   "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr)
+                 : "memory");
 }
 
 __device__ __forceinline__ int imod(int a, int n) {
@@ -245,15 +245,15 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
     uint8_t *A = smem;
     uint8_t *B = smem + G::A_BYTES;
     uint8_t *aux = B + G::B_BYTES;
-    uint64_t *bars = (uint64_t *)aux;                 // 7 barriers
+    uint64_t *bars = (uint64_t *)aux;                 // 8 barriers
     uint32_t *tslot = (uint32_t *)(aux + 64);
-    double *red = (double *)(aux + 128);              // 4 doubles
+    double *red = (double *)(aux + 128);              // 8 doubles
     int *rowE = (int *)(aux + 1024);                  // producers -> MMA issuer
     int *rowE_epi = rowE + kM;                        // MMA issuer -> epilogue, by tile parity
-    const uint32_t bA_full = saddr(&bars[0]), bA_empty = saddr(&bars[1]),
-                   bT_full0 = saddr(&bars[2]), bT_full1 = saddr(&bars[3]),
-                   bT_empty0 = saddr(&bars[4]), bT_empty1 = saddr(&bars[5]),
-                   bX_full = saddr(&bars[6]);
+    const uint32_t bA_full = saddr(&bars[0]), bA_empty = saddr(&bars[1]);
+    const uint32_t bT_full[2] = {saddr(&bars[2]), saddr(&bars[3])};
+    const uint32_t bT_empty[2] = {saddr(&bars[4]), saddr(&bars[5])};
+    const uint32_t bX_full[2] = {saddr(&bars[6]), saddr(&bars[7])};
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const long long nlines = (long long)S.nL * S.nR;
@@ -273,16 +273,16 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (tid == 0) {
-        bar_init(bA_full, 128);
+        bar_init(bA_full, kProducers);
         bar_init(bA_empty, 1);
-        bar_init(bT_full0, 1);
-        bar_init(bT_full1, 1);
-        bar_init(bT_empty0, 128);
-        bar_init(bT_empty1, 128);
-        bar_init(bX_full, 1);
+        for (int h = 0; h < 2; ++h) {
+            bar_init(bT_full[h], 1);
+            bar_init(bT_empty[h], 128);
+            bar_init(bX_full[h], 1);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    if (tid < 4) red[tid] = 0.0;
+    if (tid < 8) red[tid] = 0.0;
     // Toeplitz filter tiles B_t[n][kk] = e_t(kk - n), K-major core matrices
     for (int idx = tid; idx < G::ND * 16 * G::KB; idx += kThreads) {
         const int t = idx / (16 * G::KB), rem = idx % (16 * G::KB);
@@ -301,18 +301,22 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
 
     const uint64_t a_desc0 = umma_desc(saddr(A), 2048, 128);
     const uint64_t b_desc0 = umma_desc(saddr(B), 256, 128);
-    if (warp < 4) {
-        // ================================ producers (+ MMA issue in warp 0)
-        uint32_t it = 0;
+    if (warp < kProducers / 32) {
+        // ============ producers: thread = (row, half of the row segment);
+        // half-warps cover 16 consecutive rows, lanes 0-15 positions [0, KT/2),
+        // lanes 16-31 [KT/2, KT).  Pass 1 finds the row's largest exponent,
+        // pass 2 re-reads the values (L1) and writes their byte digits.
+        constexpr int H = G::KT / 2;                                  // multiple of 8
+        const int half = lane >> 4;
+        const int row = warp * 16 + (lane & 15);
         const long long *xbits = reinterpret_cast<const long long *>(S.x);
+        uint32_t it = 0;
         for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
             if (it > 0 && !bar_wait(bA_empty, (it - 1) & 1)) { alive = false; break; }
             const int ch = (int)(tile % nch);
             const long long lb = (tile / nch) % nlb;
             const int arr = (int)(tile / (nch * nlb));
             const int p0 = S.qlo + ch * kQC + S.lowfil;
-            // periodic: start of the segment in [0, n); a segment wraps at most
-            // once when n >= KT, otherwise the slow modulo is used
             const int pstart = S.bc == BC_PERIODIC ? imod(p0, S.n) : 0;
             const bool onewrap = S.n >= G::KT;
             auto pos_of = [&](int kk) -> int {       // array position, -1 for a zero
@@ -325,113 +329,125 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
                 if (S.bc == BC_SHRINK) return p - S.in_lo;
                 return (p < 0 || p >= S.n) ? -1 : p;
             };
-            // thread = (row, half of the row segment): half-warps cover 16 rows,
-            // lanes 0-15 hold positions [0, KT/2), lanes 16-31 [KT/2, KT)
-            constexpr int H = G::KT / 2;                          // multiple of 8
-            const int half = lane >> 4;
-            for (int rb = 0; rb < 32; rb += 16) {
-                const int row = warp * 32 + rb + (lane & 15);
-                const long long g = lb * kM + row;
-                const bool valid = g < nlines;
-                const long long l = valid ? g % S.nL : 0, r = valid ? g / S.nL : 0;
-                const long long *base = xbits + (long long)arr * S.x_arr + l + (long long)S.nL * (long long)S.in_ext * r;
-                const long long stride = S.nL;
-                long long bits[H];
-                // contiguous fast path: the needed part of the half segment,
-                // [k0, k0 + len), is one unbroken, 16-byte aligned run of array
-                // positions -> vector loads (+ one scalar tail); zeros beyond
-                const int k0 = half * H;
-                const int klim = min(kneed, plast - p0 + 1);       // positions any output needs
-                const int len = max(0, min(H, klim - k0));
-                const int ps0 = len > 0 ? pos_of(k0) : -1;
-                const int psl = len > 0 ? pos_of(k0 + len - 1) : -1;
-                const bool run = valid && stride == 1 && ps0 >= 0 && psl == ps0 + len - 1 &&
-                                 ((((uintptr_t)(base + ps0)) & 15) == 0);
+            const long long g = lb * kM + row;
+            const bool valid = g < nlines;
+            const long long l = valid ? g % S.nL : 0, r = valid ? g / S.nL : 0;
+            const long long *base = xbits + (long long)arr * S.x_arr + l + (long long)S.nL * (long long)S.in_ext * r;
+            const long long stride = S.nL;
+            const int k0 = half * H;
+            const int klim = min(kneed, plast - p0 + 1);
+            const int len = max(0, min(H, klim - k0));
+            const int ps0 = (valid && len > 0) ? pos_of(k0) : -1;
+            const int psl = (valid && len > 0) ? pos_of(k0 + len - 1) : -1;
+            // contiguous fast path: [k0, k0+len) is one unbroken 16-byte aligned run
+            const bool run = stride == 1 && ps0 >= 0 && psl == ps0 + len - 1 &&
+                             ((((uintptr_t)(base + ps0)) & 15) == 0);
+            auto load8 = [&](int c, long long (&bits)[8]) {
                 if (run) {
                     const double2 *v = reinterpret_cast<const double2 *>(base + ps0);
 #pragma unroll
-                    for (int e = 0; e < H / 2; ++e) {
-                        if (2 * e + 1 < len) {
-                            const double2 t = v[e];
+                    for (int e = 0; e < 4; ++e) {
+                        const int i = c * 8 + 2 * e;
+                        if (i + 1 < len) {
+                            const double2 t = v[c * 4 + e];
                             bits[2 * e] = __double_as_longlong(t.x);
                             bits[2 * e + 1] = __double_as_longlong(t.y);
                         } else {
-                            bits[2 * e] = 2 * e < len ? base[ps0 + 2 * e] : 0ll;
+                            bits[2 * e] = i < len ? base[ps0 + i] : 0ll;
                             bits[2 * e + 1] = 0ll;
                         }
                     }
                 } else {
 #pragma unroll
-                    for (int e = 0; e < H; ++e) {
-                        const int ps = valid ? pos_of(k0 + e) : -1;
+                    for (int e = 0; e < 8; ++e) {
+                        const int ps = valid ? pos_of(k0 + c * 8 + e) : -1;
                         bits[e] = ps >= 0 ? base[(long long)ps * stride] : 0ll;
                     }
                 }
-                int mx = 0;
+            };
+            int mx = 0;
 #pragma unroll
-                for (int e = 0; e < H; ++e) mx = max(mx, (int)(((unsigned long long)bits[e] >> 52) & 0x7FF));
-                mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
-                const int E = (mx ? mx : 1) - 1022;
+            for (int c0 = 0; c0 < H / 8; c0 += 2) {          // 16 loads in flight
+                long long b0[8], b1[8];
+                load8(c0, b0);
+                if (c0 + 1 < H / 8) load8(c0 + 1, b1);
+                else {
 #pragma unroll
-                for (int c = 0; c < H / 8; ++c) {
-                    uint32_t xl[8], xh[8], sg[8];
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) fixed64(bits[c * 8 + e], E, xl[e], xh[e], sg[e]);
-                    uint32_t smul[4], sadd[4];
-#pragma unroll
-                    for (int w = 0; w < 4; ++w) {
-                        smul[w] = (0x3C00u | (sg[2 * w] << 15)) | ((0x3C00u | (sg[2 * w + 1] << 15)) << 16);
-                        sadd[w] = (0xE400u ^ (sg[2 * w] << 15)) | ((0xE400u ^ (sg[2 * w + 1] << 15)) << 16);
-                    }
-                    const int off = (half * (H / 8) + c) * 2048 + (row >> 3) * 128 + (row & 7) * 16;
-#pragma unroll
-                    for (int sd = 0; sd < G::ND; ++sd) {
-                        uint32_t wds[4];
-#pragma unroll
-                        for (int w = 0; w < 4; ++w)
-                            wds[w] = digit_pair(7 - sd, xl[2 * w], xh[2 * w], xl[2 * w + 1], xh[2 * w + 1],
-                                                smul[w], sadd[w]);
-                        *(uint4 *)(A + sd * G::A_PLANE + off) = make_uint4(wds[0], wds[1], wds[2], wds[3]);
-                    }
+                    for (int e = 0; e < 8; ++e) b1[e] = 0ll;
                 }
-                if (half == 0) rowE[row] = mx == 0x7FF ? 0x7FFFFFFF : E;
+#pragma unroll
+                for (int e = 0; e < 8; ++e)
+                    mx = max(mx, max((int)(((unsigned long long)b0[e] >> 52) & 0x7FF),
+                                     (int)(((unsigned long long)b1[e] >> 52) & 0x7FF)));
             }
+            mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
+            const int E = (mx ? mx : 1) - 1022;
+#pragma unroll 1
+            for (int c = 0; c < H / 8; ++c) {
+                long long bits[8];
+                load8(c, bits);
+                uint32_t xl[8], xh[8], sg[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) fixed64(bits[e], E, xl[e], xh[e], sg[e]);
+                uint32_t smul[4], sadd[4];
+#pragma unroll
+                for (int w = 0; w < 4; ++w) {
+                    smul[w] = (0x3C00u | (sg[2 * w] << 15)) | ((0x3C00u | (sg[2 * w + 1] << 15)) << 16);
+                    sadd[w] = (0xE400u ^ (sg[2 * w] << 15)) | ((0xE400u ^ (sg[2 * w + 1] << 15)) << 16);
+                }
+                const int off = (half * (H / 8) + c) * 2048 + (row >> 3) * 128 + (row & 7) * 16;
+#pragma unroll
+                for (int sd = 0; sd < G::ND; ++sd) {
+                    uint32_t wds[4];
+#pragma unroll
+                    for (int w = 0; w < 4; ++w)
+                        wds[w] = digit_pair(7 - sd, xl[2 * w], xh[2 * w], xl[2 * w + 1], xh[2 * w + 1],
+                                            smul[w], sadd[w]);
+                    *(uint4 *)(A + sd * G::A_PLANE + off) = make_uint4(wds[0], wds[1], wds[2], wds[3]);
+                }
+            }
+            if (half == 0) rowE[row] = mx == 0x7FF ? 0x7FFFFFFF : E;
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             bar_arrive(bA_full);
             if (warp == 0) {
                 // ---- MMA issue for this tile, one TMEM half at a time
                 if (!bar_wait(bA_full, it & 1)) { alive = false; break; }
-                if (it > 0 && !bar_wait(bT_empty0, (it - 1) & 1)) { alive = false; break; }
+                if (it > 0 && !bar_wait(bT_empty[0], (it - 1) & 1)) { alive = false; break; }
 #pragma unroll
                 for (int i = 0; i < kM / 32; ++i)
                     rowE_epi[(it & 1) * kM + lane + 32 * i] = rowE[lane + 32 * i];
                 __syncwarp();
                 if (lane == 0) {
-                    bar_arrive(bX_full);
+                    bar_arrive(bX_full[0]);
                     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                     issue_half<NT, 0>(tmem, a_desc0, b_desc0);
-                    commit(bT_full0);
+                    commit(bT_full[0]);
                 }
                 __syncwarp();
-                if (it > 0 && !bar_wait(bT_empty1, (it - 1) & 1)) { alive = false; break; }
+                if (it > 0 && !bar_wait(bT_empty[1], (it - 1) & 1)) { alive = false; break; }
                 if (lane == 0) {
+                    bar_arrive(bX_full[1]);
                     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                     issue_half<NT, 1>(tmem, a_desc0, b_desc0);
-                    commit(bT_full1);
+                    commit(bT_full[1]);
                     commit(bA_empty);
                 }
                 __syncwarp();
             }
         }
-    } else if (warp < 8) {
-        // ================================ epilogue
-        const int lq = warp - 4;
+    } else {
+        // ============ epilogue: warp group hf drains TMEM half hf (output blocks
+        // 2hf, 2hf+1); thread = TMEM lane = tile row; 8 outputs per step
+        const int ew = warp - kProducers / 32;
+        const int lq = ew & 3, hf = ew >> 2;
         const int row = lq * 32 + lane;
         double dot = 0.0;
         uint32_t it = 0;
         for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
-            if (!bar_wait(bX_full, it & 1)) { alive = false; break; }
+            if (!bar_wait(bX_full[hf], it & 1)) { alive = false; break; }
             const int Er = rowE_epi[(it & 1) * kM + row];
+            if (!bar_wait(bT_full[hf], it & 1)) { alive = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             const int ch = (int)(tile % nch);
             const long long lb = (tile / nch) % nlb;
             const int arr = (int)(tile / (nch * nlb));
@@ -443,33 +459,30 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
             const double *__restrict__ xa = S.x + (long long)arr * S.x_arr;
             const double *__restrict__ x2 = S.x2 ? S.x2 + (long long)arr * S.x_arr : nullptr;
             const int se = Er + F.ef - 56;
-            for (int j = 0; j < kNB; ++j) {
-                if ((j & 1) == 0) {                 // entering TMEM half j/2
-                    if (!bar_wait(j ? bT_full1 : bT_full0, it & 1)) { alive = false; break; }
-                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                }
-                uint32_t acc[G::ORD][16];
+#pragma unroll 1
+            for (int step = 0; step < 4; ++step) {             // 2 blocks x 2 x 8 outputs
+                const int jj = step >> 1, n0 = (step & 1) * 8;
+                uint32_t acc[G::ORD][8];
 #pragma unroll
                 for (int k = 0; k < G::ORD; ++k)
-                    tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) +
-                                  (uint32_t)((j >> 1) * G::HALF_COLS + ((j & 1) * G::ORD + k) * 16),
-                              acc[k]);
+                    tmem_ld8(tmem + ((uint32_t)(lq * 32) << 16) +
+                                 (uint32_t)(hf * G::HALF_COLS + (jj * G::ORD + k) * 16 + n0),
+                             acc[k]);
                 asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                if (j & 1) {                        // half drained: release it
+                if (step == 3) {                                // half drained: release it
                     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-                    bar_arrive(j == 1 ? bT_empty0 : bT_empty1);
+                    bar_arrive(bT_empty[hf]);
                 }
                 if (!valid) continue;
-                const int q0 = qc0 + 16 * j;
-                const int nv = S.qhi - q0 + 1 < 16 ? S.qhi - q0 + 1 : 16;   // outputs in this block
+                const int q0 = qc0 + 16 * (2 * hf + jj) + n0;
+                const int nv = min(8, S.qhi - q0 + 1);
                 if (nv <= 0) continue;
-                double add[16];
-                const bool full = nv == 16;
+                double add[8];
 #pragma unroll
-                for (int n = 0; n < 16; ++n) {
+                for (int n = 0; n < 8; ++n) {
                     add[n] = 0.0;
-                    const int q = q0 + n;
-                    if (x2 && (full || n < nv)) {
+                    if (x2 && n < nv) {
+                        const int q = q0 + n;
                         const long long pos = q - S.out_lo;
                         const long long x2i = S.bc == BC_GROW
                             ? (S.transpose ? rr + (long long)S.nR * pos : l + (long long)S.nL * (pos + (long long)S.out_ext * rr))
@@ -478,8 +491,8 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
                     }
                 }
 #pragma unroll
-                for (int n = 0; n < 16; ++n) {
-                    if (!full && n >= nv) break;
+                for (int n = 0; n < 8; ++n) {
+                    if (n >= nv) break;
                     const int q = q0 + n;
                     long long Y = 0;
 #pragma unroll
@@ -505,11 +518,10 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
                     y[yi] = out;
                 }
             }
-            if (!alive) break;
         }
         if (S.has_dot) {
             for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
-            if (lane == 0) red[lq] = dot;
+            if (lane == 0) red[ew] = dot;
         }
     }
 
@@ -520,7 +532,11 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
                      "r"(kTmemCols)
                      : "memory");
-    if (S.has_dot && tid == 0) S.dot_part[blockIdx.x] = red[0] + red[1] + red[2] + red[3];
+    if (S.has_dot && tid == 0) {
+        double sdot = 0.0;
+        for (int i = 0; i < 8; ++i) sdot += red[i];
+        S.dot_part[blockIdx.x] = sdot;
+    }
 }
 
 int g_sms[64] = {0};
