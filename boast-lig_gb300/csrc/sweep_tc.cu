@@ -122,12 +122,16 @@ __device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait for the phase of the given parity; false after ~2 s.
+// Bounded wait for the phase of the given parity; false after ~2 s.  Between
+// polls the warp sleeps briefly so waiting warps leave the issue slots to the
+// working ones.
 __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
     if (bar_try(bar, parity)) return true;
     const long long t0 = clock64();
-    while (!bar_try(bar, parity))
+    while (!bar_try(bar, parity)) {
+        __nanosleep(128);
         if (clock64() - t0 > kWaitCycles) return false;
+    }
     return true;
 }
 
@@ -144,28 +148,15 @@ __device__ __forceinline__ int imod(int a, int n) {
     return r < 0 ? r + n : r;
 }
 
-// int64 Y times 2^se as an FP64, rounded to nearest even, built from the bits.
-__device__ __forceinline__ double scaled_to_f64(long long Y, int se) {
-    if (Y == 0) return 0.0;
-    const unsigned long long neg = Y < 0 ? (1ull << 63) : 0ull;
-    unsigned long long m = Y < 0 ? (unsigned long long)(-Y) : (unsigned long long)Y;
-    const int lz = __clzll((long long)m);
-    m <<= lz;
-    unsigned long long mant = m >> 11;
-    const unsigned rem = (unsigned)(m & 0x7FF);
-    mant += (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
-    int e = 63 - lz + se;
-    if (mant >> 53) { mant >>= 1; ++e; }
-    if (e > 1023) return __longlong_as_double((long long)(neg | 0x7FF0000000000000ull));   // overflow
-    if (e < -1022) {                                   // subnormal (re-rounded) or zero
-        const int sh = -1022 - e;
-        mant = sh >= 54 ? 0ull : (mant + ((1ull << sh) >> 1)) >> sh;
-        return __longlong_as_double((long long)(neg | mant));
-    }
-    return __longlong_as_double((long long)(neg | ((unsigned long long)(e + 1023) << 52) |
-                                            (mant & 0xFFFFFFFFFFFFFull)));
+// d * 2^se for an FP64 d produced from an integer (exact when the result is a
+// normal number: the exponent field is adjusted with one integer add).
+__device__ __forceinline__ double scale_pow2(double d, int se) {
+    const long long b = __double_as_longlong(d);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e == 0) return d;                                      // zero
+    if (e + se >= 1 && e + se <= 2046) return __longlong_as_double(b + ((long long)se << 52));
+    return ldexp(d, se);                                       // result outside the normal range
 }
-
 
 // Fixed-point magnitude |X| = round(|x| 2^(64-E)) of the FP64 bit pattern
 // (|x| < 2^E), split in 32-bit words, and the sign bit.  Integer only:
@@ -494,15 +485,16 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
                 for (int n = 0; n < 8; ++n) {
                     if (n >= nv) break;
                     const int q = q0 + n;
-                    long long Y = 0;
+                    // Y = sum_{k<=5} Acc_k 2^(8(5-k)) + Acc_6 2^-8 (+ Acc_7 2^-16), Horner form
+                    long long Y = __float2int_rn(__uint_as_float(acc[0][n]));
 #pragma unroll
-                    for (int k = 0; k < 6; ++k)
-                        Y += (long long)__float2int_rn(__uint_as_float(acc[k][n])) << (8 * (5 - k));
-                    Y += ((long long)__float2int_rn(__uint_as_float(acc[6][n])) + 128) >> 8;
-                    if (G::ORD > 7)
-                        Y += ((long long)__float2int_rn(__uint_as_float(acc[G::ORD - 1][n])) + 32768) >> 16;
+                    for (int k = 1; k < 6; ++k)
+                        Y = Y * 256 + __float2int_rn(__uint_as_float(acc[k][n]));
+                    int lo = __float2int_rn(__uint_as_float(acc[6][n]));
+                    if (G::ORD > 7) lo += (__float2int_rn(__uint_as_float(acc[G::ORD - 1][n])) + 128) >> 8;
+                    Y += ((long long)lo + 128) >> 8;
                     double out = Er == 0x7FFFFFFF ? __longlong_as_double(0x7FF8000000000000LL)
-                                                  : scaled_to_f64(Y, se);
+                                                  : scale_pow2(__ll2double_rn(Y), se);
                     const long long pos = q - S.out_lo;
                     const long long yi = S.transpose ? rr + (long long)S.nR * pos
                                                      : l + (long long)S.nL * (pos + (long long)S.out_ext * rr);
