@@ -450,6 +450,44 @@ int cost_md(const OpDef &op, int d, const int *n, const int *bc, int narr, long 
 
 }  // namespace
 
+namespace lcg {
+// Validation and geometry of one 1D kinetic sweep with dot_in (the plan_1d
+// restatement for OP_D2), filled into S without any container or allocation;
+// used by the allocation-free entry point.
+int kinetic_dotin_sweep(int d, int idim, const int *n, int bc, const int *nx, const int *ny,
+                        int narr, double a, double a_x, double a_y, Sweep &S) {
+    if (d < 1 || idim < 0 || idim >= d) return fail(LIBCONV_EARG, "d=%d idim=%d", d, idim);
+    if (!n || !nx || !ny) return fail(LIBCONV_EARG, "n/nx/ny must not be null");
+    if (narr < 1 || narr > 65535) return fail(LIBCONV_EARG, "narr=%d out of [1,65535]", narr);
+    if (!bc_valid(bc)) return fail(LIBCONV_EBC, "unknown boundary condition %d", bc);
+    for (int i = 0; i < d; ++i)
+        if (n[i] < 1 || nx[i] < 1 || ny[i] < 1)
+            return fail(LIBCONV_EARG, "n/nx/ny[%d] must be >= 1", i);
+    if (nx[idim] < need_in(OP_D2, bc, n[idim]) || ny[idim] < need_out(OP_D2, bc, n[idim]))
+        return fail(LIBCONV_ESIZE, "nx[%d]=%d / ny[%d]=%d too small for n=%d bc=%d", idim, nx[idim],
+                    idim, ny[idim], n[idim], bc);
+    long long nL = 1, nR = 1;
+    for (int i = 0; i < idim; ++i) nL *= nx[i];
+    for (int i = idim + 1; i < d; ++i) nR *= nx[i];
+    if (nL * nR > (1LL << 31) - 1) return fail(LIBCONV_EARG, "too many lines");
+    geometry(OP_D2, bc, (int)nL, n[idim], (int)nR, nx[idim], ny[idim], S);
+    S.narr = narr;
+    S.x_arr = (long long)nx[idim] * nL * nR;
+    S.y_arr = (long long)ny[idim] * nL * nR;
+    S.has_a = a != 1.0;
+    S.a = a;
+    S.has_ax = a_x != 0.0;
+    S.a_x = a_x;
+    S.ay_mode = a_y != 0.0 ? 1 : 0;
+    S.a_y = a_y;
+    S.has_dot = 1;
+    return LIBCONV_OK;
+}
+
+int report(int code, const char *msg) { return fail(code, "%s", msg); }
+int report_cuda(cudaError_t e, const char *what) { return cuda_fail(e, what); }
+}  // namespace lcg
+
 // =============================== exported C ABI ===============================
 extern "C" {
 

@@ -132,6 +132,26 @@ int d_s0s1_1d_symicomb8_dev(int d, int idim, const int *n, int bc, const int *nx
                             int narr, const double *x, double *y, double a, double a_y,
                             void *stream);
 
+/* No counterpart in the reference.  Allocation-free form of
+ * d_s0s0_1d_sym8_d2_dotin_dev, for callers that must not allocate device
+ * memory: applications whose device memory is wholly owned by their own
+ * allocator or memory budget, and latency-sensitive inner loops where a
+ * cudaMalloc/cudaFree (which can synchronise the device) is not acceptable.
+ * x, y and dot_in are caller-owned device memory; the per-block partial sums
+ * of dot_in live in a fixed device array inside the library (65536 doubles,
+ * 512 KB, held on every GPU that loads the library until exit), so a sweep
+ * needing more than 65536 partial sums (number of lines / 32, times
+ * ceil(outputs / 64), times narr) is rejected with LIBCONV_ESIZE.
+ * The first call on a device looks up that array's device address (a CUDA
+ * runtime query, done once per device, with the device current); make the
+ * first call before any stream capture.  Calls share the array: calls that
+ * overlap on the GPU (different streams, concurrently) race.  Always runs the
+ * FP64 sweep kernel, whatever the compute mode. */
+int d_s0s0_1d_sym8_d2_dotin_noalloc(int d, int idim, const int *n, int bc, const int *nx,
+                                    const int *ny, int narr, const double *x, double *y,
+                                    double a, double a_x, double a_y, double *dot_in,
+                                    void *stream);
+
 /* ---------------------------------------------------------------------
  * Multi-dimensional operators: GenericConvolutionOperator#procedure
  * (BigDFT/GenericConvolution2.rb:1934-2243).
