@@ -27,6 +27,8 @@ HEADER = os.path.join(HERE, '..', 'include', 'libconv_gb300.h')
 BC_SHRINK, BC_PERIODIC, BC_GROW, BC_FREE = -1, 0, 1, 2
 MODE_FP64 = 0
 MODE_TC_EXACT = 1
+MODE_TC_BF16X3 = 2
+MODE_TC_TF32X3 = 3
 
 _I = ctypes.POINTER(ctypes.c_int)
 _D = ctypes.POINTER(ctypes.c_double)

@@ -1,25 +1,44 @@
-// Tensor-core (tcgen05) FP64-accurate sweep: filter digits and launcher.
+// Tensor-core (tcgen05) sweeps: operand schemes, filter digits and launchers.
 #pragma once
 #include <cuda_runtime.h>
+#include <stdint.h>
 
 #include "lcg_sweep.cuh"
 
 namespace lcg {
 
-// Signed byte digits of the 64-bit fixed-point filter (operator scalar folded
-// in exactly), as FP16 bit patterns: a*tap = 2^(ef-64) * sum_s dig[s] 256^(7-s).
+// Operand schemes of the tensor-core sweep.
+enum Scheme { SCH_EXACT = 0, SCH_BF16X3 = 1, SCH_TF32X3 = 2 };
+
+// Filter operand planes, one entry per tap of the flat filter (convolution:
+// the taps; wavelets: LE | LO | HE | HO), operator scalar folded in.
+//   SCH_EXACT: signed byte digits of the 64-bit fixed point as FP16 bit
+//     patterns, a*tap = 2^(ef-64) * sum_s dig[s] 256^(7-s);
+//   SCH_BF16X3: three bfloat16 terms (low 16 bits of dig[0..2]);
+//   SCH_TF32X3: two tf32 terms (FP32 bit patterns in dig[0..1]).
 struct TcFilter {
     static constexpr int kSlices = 8;
-    static constexpr int kMaxTaps = 32;
-    unsigned short dig[kSlices][kMaxTaps];
+    static constexpr int kMaxTaps = 64;
+    uint32_t dig[kSlices][kMaxTaps];
     int ef;
 };
 
-// Host: digits of a * taps[0..ntaps).
+// Host: operand planes of a * taps[0..ntaps) for scheme sch.
 void tc_filter_digits(const double *taps, int ntaps, double a, TcFilter &F);
+void tc_filter_split(const double *taps, int ntaps, double a, int sch, TcFilter &F);
 bool sweep_tc_supported(const Sweep &S);
 long long sweep_tc_blocks(const Sweep &S);
 // status (device int) is set non-zero if a tensor-core wait timed out.
-cudaError_t launch_sweep_tc(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st);
+cudaError_t launch_sweep_tc(const Sweep &S, const TcFilter &F, int sch, int *status,
+                            cudaStream_t st);
+
+namespace tck {
+long long tile_count_for(const Sweep &S, int qp);
+int sm_count();
+// Per-scheme launchers (one translation unit each).
+cudaError_t launch_exact(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st);
+cudaError_t launch_bf16x3(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st);
+cudaError_t launch_tf32x3(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st);
+}  // namespace tck
 
 }  // namespace lcg

@@ -25,6 +25,11 @@ namespace {
 thread_local std::string t_err;
 thread_local int t_mode = LIBCONV_MODE_FP64;
 
+bool valid_mode(int m) {
+    return m == LIBCONV_MODE_FP64 || m == LIBCONV_MODE_TC_EXACT || m == LIBCONV_MODE_TC_BF16X3 ||
+           m == LIBCONV_MODE_TC_TF32X3;
+}
+
 int fail(int code, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
 int fail(int code, const char *fmt, ...) {
     char buf[512];
@@ -318,8 +323,7 @@ int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, do
 // dot product (device) when the plan has one; `scratch` holds the partials.
 int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, double *dot_dev,
              int *status, cudaStream_t st) {
-    if (t_mode != LIBCONV_MODE_FP64 && t_mode != LIBCONV_MODE_TC_EXACT)
-        return fail(LIBCONV_EMODE, "unknown mode %d", t_mode);
+    if (!valid_mode(t_mode)) return fail(LIBCONV_EMODE, "unknown mode %d", t_mode);
     for (const PlanStep &ps : P.steps) {
         Sweep S = ps.S;
         S.x = bufs[ps.src];
@@ -327,7 +331,7 @@ int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, double *dot_
         S.x2 = ps.src2 >= 0 ? bufs[ps.src2] : nullptr;
         if (!S.x || !S.y || (ps.src2 >= 0 && !S.x2))
             return fail(LIBCONV_EARG, "null device buffer in plan");
-        const bool tc = t_mode == LIBCONV_MODE_TC_EXACT && sweep_tc_supported(S);
+        const bool tc = t_mode != LIBCONV_MODE_FP64 && sweep_tc_supported(S);
         long long nb = 0;
         if (S.has_dot) {
             nb = tc ? sweep_tc_blocks(S) : sweep_fp64_blocks(S);
@@ -338,9 +342,14 @@ int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, double *dot_
         cudaError_t e;
         if (tc) {
             TcFilter F;
-            tc_filter_digits(h_ftab + S.ftab, S.ntaps, S.has_a ? S.a : 1.0, F);
-            S.has_a = 0;   // folded exactly into the filter digits
-            e = launch_sweep_tc(S, F, status, st);
+            const int sch = t_mode == LIBCONV_MODE_TC_EXACT    ? SCH_EXACT
+                            : t_mode == LIBCONV_MODE_TC_BF16X3 ? SCH_BF16X3
+                                                               : SCH_TF32X3;
+            const int flat = S.kind == KCONV ? S.ntaps : 4 * S.ntaps;   // LE|LO|HE|HO
+            if (sch == SCH_EXACT) tc_filter_digits(h_ftab + S.ftab, flat, S.has_a ? S.a : 1.0, F);
+            else tc_filter_split(h_ftab + S.ftab, flat, S.has_a ? S.a : 1.0, sch, F);
+            S.has_a = 0;   // folded into the filter operands
+            e = launch_sweep_tc(S, F, sch, status, st);
         } else {
             e = launch_sweep_fp64(S, st);
         }
@@ -520,8 +529,7 @@ int libconv_gb300_check(void *stream) {
 }
 
 int libconv_gb300_set_mode(int mode) {
-    if (mode != LIBCONV_MODE_FP64 && mode != LIBCONV_MODE_TC_EXACT)
-        return fail(LIBCONV_EMODE, "unknown mode %d", mode);
+    if (!valid_mode(mode)) return fail(LIBCONV_EMODE, "unknown mode %d", mode);
     t_mode = mode;
     return LIBCONV_OK;
 }

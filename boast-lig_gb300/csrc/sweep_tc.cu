@@ -1,537 +1,17 @@
-// FP64-accurate convolution sweep on the tcgen05 tensor cores.
-//
-// Exact integer arithmetic on FP16 operands
-//   * each line segment of a tile (128 lines x KT positions) is scaled by the
-//     power of two above its largest magnitude to 64-bit integers |X| < 2^64;
-//     the 8 bytes of |X| are the digits d_0 (top byte) .. d_7, each held
-//     exactly in FP16 with the sign of x;
-//   * the filter, with the operator scalar a folded in exactly (128-bit
-//     product of the two mantissas), is cut the same way into bytes e_0..e_7;
-//   * every byte-pair product is below 2^16 and every partial sum over <= 29
-//     taps x 8 pairs stays below 2^24, so the FP32 accumulation of
-//     tcgen05.mma (kind::f16) is exact;
-//   * the pairs of order k = s + t <= 6 (16-tap MagicFilter: 28 pairs) or
-//     k <= 7 (29-tap kinetic / derivative filters, whose large alternating
-//     taps cancel: 36 pairs) are accumulated in TMEM, one accumulator per
-//     order; the epilogue recombines
-//        Y = sum_{k<=5} Acc_k 2^(8(5-k)) + Acc_6 / 2^8 + Acc_7 / 2^16
-//     in int64 and builds the FP64 result bit by bit (no FP64 instruction).
-//   Dropped orders weigh <= 2^-64 of the line scale: the result is at least as
-//   accurate as an FP64 FMA chain.  Lines never share a scale; a line segment
-//   holding an Inf or NaN gives NaN on that tile row.
-//
-// The convolution of one 16-output block is a banded Toeplitz product
-//   D[line, n] = sum_kk A[line, kk] * B[kk, n],   B[kk, n] = f(kk - n + lowfil)
-// with K = 32 (16 taps) or 48 (29 taps); A is a digit plane of the tile,
-// addressed at an offset of 16 positions per output block.
-//
-// Persistent, warp-specialised CTA (one per SM), 512 threads at <= 128
-// registers, one A buffer and two TMEM accumulator halves (blocks 0-1 and 2-3
-// of a tile, 256 columns each):
-//   warps 0-7  producers: thread = (row, half of the row segment): largest
-//              exponent of the row, then its byte digits into the A planes
-//              (coalesced or vector loads); warp 0 then issues the tile's MMAs
-//              (lane 0, fully unrolled, precomputed descriptors), each TMEM
-//              half as soon as the epilogue has released it;
-//   warps 8-15 epilogue: warps 8-11 drain TMEM half 0, warps 12-15 half 1;
-//              thread = TMEM lane = tile row; TMEM -> FP64 -> global.
-// Producers fill tile i+1 while the epilogue drains tile i, and the MMAs of a
-// TMEM half overlap the draining of the other.  Every hand-off is an mbarrier
-// whose phase can never run two phases ahead of its waiter, and every wait
-// gives up after ~2 s of SM clock (status word set, TMEM freed).
+// Host side of the tensor-core sweeps: filter operand planes, support test,
+// grid size and scheme dispatch.  The kernel itself is tc_kernel.cuh.
 #include <cuda_fp16.h>
-#include <stdint.h>
+#include <math.h>
+#include <string.h>
 
-#include "lcg_sweep.cuh"
 #include "lcg_tc.cuh"
 
 namespace lcg {
+namespace tck {
+
 namespace {
-
-constexpr int kM = 128;          // lines per tile (MMA M)
-constexpr int kQC = 64;          // outputs per tile
-constexpr int kNB = kQC / 16;    // 16-output blocks per tile
-constexpr int kThreads = 512;     // 8 producer warps + 8 epilogue warps
-constexpr int kProducers = 256;
-constexpr uint32_t kTmemCols = 512;
-constexpr long long kWaitCycles = 4000000000LL;
-
-template <int NT> struct TcGeom {
-    static constexpr int KB = ((16 + NT - 1) + 15) / 16 * 16;   // K per output block
-    static constexpr int KT = 16 * (kNB - 1) + KB;              // positions per tile
-    static constexpr int ORD = NT > 16 ? 8 : 7;                 // accumulated orders
-    static constexpr int ND = NT > 16 ? 8 : 7;                  // digit planes used
-    static constexpr int A_PLANE = kM * KT * 2;
-    static constexpr int B_PLANE = 16 * KB * 2;
-    static constexpr int A_BYTES = ND * A_PLANE;
-    static constexpr int B_BYTES = ND * B_PLANE;
-    static constexpr int AUX = 1024 + 3 * 4 * kM;               // barriers, slots, row exponents
-    static constexpr int SMEM = A_BYTES + B_BYTES + AUX + 1024;
-    static constexpr int HALF_COLS = 2 * ORD * 16;             // one TMEM half (2 blocks)
-    static_assert(2 * HALF_COLS <= (int)kTmemCols && HALF_COLS <= 256, "TMEM columns");
-};
-
-// ---- PTX wrappers ----------------------------------------------------------------
-__device__ __forceinline__ uint32_t saddr(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-    // K-major, no swizzle: start, leading (K-direction) and stride (8-row)
-    // byte offsets in 16-byte units; bits 46-47 = 1 (descriptor version).
-    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
-           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
-}
-
-// kind::f16 instruction descriptor: D F32, A/B F16, both K-major, N = 16, M = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((16u >> 3) << 17) |
-                            ((uint32_t)(kM >> 4) << 24);
-
-__device__ __forceinline__ void mma_f16(uint32_t d, uint64_t a, uint64_t b, uint32_t accum) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-        "l"(a), "l"(b), "r"(kIdesc), "r"(accum)
-        : "memory");
-}
-
-__device__ __forceinline__ void commit(uint32_t bar) {
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
-        : "memory");
-}
-
-__device__ __forceinline__ void bar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void bar_arrive(uint32_t bar) {
-    asm volatile(
-        "{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(bar)
-        : "memory");
-}
-
-__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait for the phase of the given parity; false after ~2 s.  Between
-// polls the warp sleeps briefly so waiting warps leave the issue slots to the
-// working ones.
-__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
-    if (bar_try(bar, parity)) return true;
-    const long long t0 = clock64();
-    while (!bar_try(bar, parity)) {
-        __nanosleep(128);
-        if (clock64() - t0 > kWaitCycles) return false;
-    }
-    return true;
-}
-
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-                   "=r"(r[6]), "=r"(r[7])
-                 : "r"(taddr)
-                 : "memory");
-}
-
-__device__ __forceinline__ int imod(int a, int n) {
-    int r = a % n;
-    return r < 0 ? r + n : r;
-}
-
-// d * 2^se for an FP64 d produced from an integer (exact when the result is a
-// normal number: the exponent field is adjusted with one integer add).
-__device__ __forceinline__ double scale_pow2(double d, int se) {
-    const long long b = __double_as_longlong(d);
-    const int e = (int)((b >> 52) & 0x7FF);
-    if (e == 0) return d;                                      // zero
-    if (e + se >= 1 && e + se <= 2046) return __longlong_as_double(b + ((long long)se << 52));
-    return ldexp(d, se);                                       // result outside the normal range
-}
-
-// Fixed-point magnitude |X| = round(|x| 2^(64-E)) of the FP64 bit pattern
-// (|x| < 2^E), split in 32-bit words, and the sign bit.  Integer only:
-// left shifts (values within 2^11 of the row maximum) are two funnel shifts.
-__device__ __forceinline__ void fixed64(long long bits, int E, uint32_t &xl, uint32_t &xh,
-                                        uint32_t &sgn) {
-    const uint32_t lo = (uint32_t)bits, hi = (uint32_t)((unsigned long long)bits >> 32);
-    int ex = (int)((hi >> 20) & 0x7FF);
-    uint32_t mh = hi & 0xFFFFFu;
-    if (ex) mh |= 0x100000u;
-    else ex = 1;
-    sgn = hi >> 31;
-    const int r = E - (ex - 1022);                       // |X| = mant 2^(11 - r)
-    if (r <= 11) {
-        const uint32_t c = (uint32_t)(11 - r);           // 0..11
-        xh = __funnelshift_l(lo, mh, c);
-        xl = lo << c;
-    } else {
-        const int c = r - 11;                            // right shift with rounding
-        if (c >= 64) { xl = xh = 0; return; }
-        unsigned long long m = ((unsigned long long)mh << 32) | lo;
-        m = (m + (1ull << (c - 1))) >> c;
-        xl = (uint32_t)m;
-        xh = (uint32_t)(m >> 32);
-    }
-}
-
-// half2 of byte b (0 = lowest) of two fixed-point magnitudes, with their
-// signs: PRMT gathers the bytes, 0x6400 makes them 1024 + d in FP16, and one
-// HFMA2 applies +-1 and removes the 1024 (exact).
-__device__ __forceinline__ uint32_t digit_pair(int b, uint32_t al, uint32_t ah, uint32_t bl,
-                                               uint32_t bh, uint32_t smul, uint32_t sadd) {
-    const uint32_t wa = b >= 4 ? ah : al;
-    const uint32_t wb = b >= 4 ? bh : bl;
-    const uint32_t sel = (uint32_t)(b & 3) | ((uint32_t)(4 + (b & 3)) << 8);
-    uint32_t t;
-    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(t) : "r"(wa), "r"(wb), "r"(sel));
-    t = (t & 0x00FF00FFu) | 0x64006400u;
-    __half2 h = *reinterpret_cast<__half2 *>(&t);
-    h = __hfma2(h, *reinterpret_cast<const __half2 *>(&smul), *reinterpret_cast<const __half2 *>(&sadd));
-    return *reinterpret_cast<uint32_t *>(&h);
-}
-
-
-// Issue the MMAs of one TMEM half (output blocks 2h, 2h+1) of a tile.  Orders
-// k = s + t are accumulated one per 16-column accumulator; the first pair of
-// an order overwrites it.  Descriptors are advanced by adding the (16-byte
-// unit) offset to the start-address field (addresses < 256 KB never carry).
-template <int NT, int H>
-__device__ __forceinline__ void issue_half(uint32_t tmem, uint64_t a_desc0, uint64_t b_desc0) {
-    using G = TcGeom<NT>;
-#pragma unroll
-    for (int jj = 0; jj < 2; ++jj)
-#pragma unroll
-        for (int k = 0; k < G::ORD; ++k) {
-            const uint32_t d = tmem + (uint32_t)(H * G::HALF_COLS + (jj * G::ORD + k) * 16);
-            constexpr int dummy = 0;
-            (void)dummy;
-#pragma unroll
-            for (int s = (k > 7 ? k - 7 : 0); s <= (k < 7 ? k : 7); ++s)
-#pragma unroll
-                for (int ks = 0; ks < G::KB / 16; ++ks) {
-                    const int j = 2 * H + jj;
-                    const uint64_t ad = a_desc0 + (uint64_t)((s * G::A_PLANE + (2 * j + 2 * ks) * 2048) >> 4);
-                    const uint64_t bd = b_desc0 + (uint64_t)(((k - s) * G::B_PLANE + 2 * ks * 256) >> 4);
-                    mma_f16(d, ad, bd, (s == (k > 7 ? k - 7 : 0) && ks == 0) ? 0u : 1u);
-                }
-        }
-}
-
-template <int NT>
-__global__ void __launch_bounds__(kThreads, 1)
-sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
-    using G = TcGeom<NT>;
-    extern __shared__ uint8_t smem_raw[];
-    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint8_t *A = smem;
-    uint8_t *B = smem + G::A_BYTES;
-    uint8_t *aux = B + G::B_BYTES;
-    uint64_t *bars = (uint64_t *)aux;                 // 8 barriers
-    uint32_t *tslot = (uint32_t *)(aux + 64);
-    double *red = (double *)(aux + 128);              // 8 doubles
-    int *rowE = (int *)(aux + 1024);                  // producers -> MMA issuer
-    int *rowE_epi = rowE + kM;                        // MMA issuer -> epilogue, by tile parity
-    const uint32_t bA_full = saddr(&bars[0]), bA_empty = saddr(&bars[1]);
-    const uint32_t bT_full[2] = {saddr(&bars[2]), saddr(&bars[3])};
-    const uint32_t bT_empty[2] = {saddr(&bars[4]), saddr(&bars[5])};
-    const uint32_t bX_full[2] = {saddr(&bars[6]), saddr(&bars[7])};
-
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const long long nlines = (long long)S.nL * S.nR;
-    const long long nlb = (nlines + kM - 1) / kM;
-    const int nq = S.qhi - S.qlo + 1;
-    const int nch = (nq + kQC - 1) / kQC;
-    const long long ntiles = nlb * nch * S.narr;
-    const int upfil = S.lowfil + NT - 1;
-    const int plast = S.qhi + upfil;
-    const int kneed = kQC + NT - 1;
-
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
-                         saddr(tslot)),
-                     "r"(kTmemCols)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
-    }
-    if (tid == 0) {
-        bar_init(bA_full, kProducers);
-        bar_init(bA_empty, 1);
-        for (int h = 0; h < 2; ++h) {
-            bar_init(bT_full[h], 1);
-            bar_init(bT_empty[h], 128);
-            bar_init(bX_full[h], 1);
-        }
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    }
-    if (tid < 8) red[tid] = 0.0;
-    // Toeplitz filter tiles B_t[n][kk] = e_t(kk - n), K-major core matrices
-    for (int idx = tid; idx < G::ND * 16 * G::KB; idx += kThreads) {
-        const int t = idx / (16 * G::KB), rem = idx % (16 * G::KB);
-        const int n = rem / G::KB, kk = rem % G::KB;
-        const int tap = kk - n;
-        const unsigned short v = (tap >= 0 && tap < NT) ? F.dig[t][tap] : (unsigned short)0;
-        *(unsigned short *)(B + t * G::B_PLANE + (kk >> 3) * 256 + (n >> 3) * 128 + (n & 7) * 16 +
-                            (kk & 7) * 2) = v;
-    }
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    const uint32_t tmem = *tslot;
-    bool alive = true;
-
-    const uint64_t a_desc0 = umma_desc(saddr(A), 2048, 128);
-    const uint64_t b_desc0 = umma_desc(saddr(B), 256, 128);
-    if (warp < kProducers / 32) {
-        // ============ producers: thread = (row, half of the row segment);
-        // half-warps cover 16 consecutive rows, lanes 0-15 positions [0, KT/2),
-        // lanes 16-31 [KT/2, KT).  Pass 1 finds the row's largest exponent,
-        // pass 2 re-reads the values (L1) and writes their byte digits.
-        constexpr int H = G::KT / 2;                                  // multiple of 8
-        const int half = lane >> 4;
-        const int row = warp * 16 + (lane & 15);
-        const long long *xbits = reinterpret_cast<const long long *>(S.x);
-        uint32_t it = 0;
-        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
-            if (it > 0 && !bar_wait(bA_empty, (it - 1) & 1)) { alive = false; break; }
-            const int ch = (int)(tile % nch);
-            const long long lb = (tile / nch) % nlb;
-            const int arr = (int)(tile / (nch * nlb));
-            const int p0 = S.qlo + ch * kQC + S.lowfil;
-            const int pstart = S.bc == BC_PERIODIC ? imod(p0, S.n) : 0;
-            const bool onewrap = S.n >= G::KT;
-            auto pos_of = [&](int kk) -> int {       // array position, -1 for a zero
-                const int p = p0 + kk;
-                if (kk >= kneed || p > plast) return -1;
-                if (S.bc == BC_PERIODIC) {
-                    if (onewrap) { const int q = pstart + kk; return q >= S.n ? q - S.n : q; }
-                    return imod(p, S.n);
-                }
-                if (S.bc == BC_SHRINK) return p - S.in_lo;
-                return (p < 0 || p >= S.n) ? -1 : p;
-            };
-            const long long g = lb * kM + row;
-            const bool valid = g < nlines;
-            const long long l = valid ? g % S.nL : 0, r = valid ? g / S.nL : 0;
-            const long long *base = xbits + (long long)arr * S.x_arr + l + (long long)S.nL * (long long)S.in_ext * r;
-            const long long stride = S.nL;
-            const int k0 = half * H;
-            const int klim = min(kneed, plast - p0 + 1);
-            const int len = max(0, min(H, klim - k0));
-            const int ps0 = (valid && len > 0) ? pos_of(k0) : -1;
-            const int psl = (valid && len > 0) ? pos_of(k0 + len - 1) : -1;
-            // contiguous fast path: [k0, k0+len) is one unbroken 16-byte aligned run
-            const bool run = stride == 1 && ps0 >= 0 && psl == ps0 + len - 1 &&
-                             ((((uintptr_t)(base + ps0)) & 15) == 0);
-            auto load8 = [&](int c, long long (&bits)[8]) {
-                if (run) {
-                    const double2 *v = reinterpret_cast<const double2 *>(base + ps0);
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const int i = c * 8 + 2 * e;
-                        if (i + 1 < len) {
-                            const double2 t = v[c * 4 + e];
-                            bits[2 * e] = __double_as_longlong(t.x);
-                            bits[2 * e + 1] = __double_as_longlong(t.y);
-                        } else {
-                            bits[2 * e] = i < len ? base[ps0 + i] : 0ll;
-                            bits[2 * e + 1] = 0ll;
-                        }
-                    }
-                } else {
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) {
-                        const int ps = valid ? pos_of(k0 + c * 8 + e) : -1;
-                        bits[e] = ps >= 0 ? base[(long long)ps * stride] : 0ll;
-                    }
-                }
-            };
-            int mx = 0;
-#pragma unroll
-            for (int c0 = 0; c0 < H / 8; c0 += 2) {          // 16 loads in flight
-                long long b0[8], b1[8];
-                load8(c0, b0);
-                if (c0 + 1 < H / 8) load8(c0 + 1, b1);
-                else {
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) b1[e] = 0ll;
-                }
-#pragma unroll
-                for (int e = 0; e < 8; ++e)
-                    mx = max(mx, max((int)(((unsigned long long)b0[e] >> 52) & 0x7FF),
-                                     (int)(((unsigned long long)b1[e] >> 52) & 0x7FF)));
-            }
-            mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
-            const int E = (mx ? mx : 1) - 1022;
-#pragma unroll 1
-            for (int c = 0; c < H / 8; ++c) {
-                long long bits[8];
-                load8(c, bits);
-                uint32_t xl[8], xh[8], sg[8];
-#pragma unroll
-                for (int e = 0; e < 8; ++e) fixed64(bits[e], E, xl[e], xh[e], sg[e]);
-                uint32_t smul[4], sadd[4];
-#pragma unroll
-                for (int w = 0; w < 4; ++w) {
-                    smul[w] = (0x3C00u | (sg[2 * w] << 15)) | ((0x3C00u | (sg[2 * w + 1] << 15)) << 16);
-                    sadd[w] = (0xE400u ^ (sg[2 * w] << 15)) | ((0xE400u ^ (sg[2 * w + 1] << 15)) << 16);
-                }
-                const int off = (half * (H / 8) + c) * 2048 + (row >> 3) * 128 + (row & 7) * 16;
-#pragma unroll
-                for (int sd = 0; sd < G::ND; ++sd) {
-                    uint32_t wds[4];
-#pragma unroll
-                    for (int w = 0; w < 4; ++w)
-                        wds[w] = digit_pair(7 - sd, xl[2 * w], xh[2 * w], xl[2 * w + 1], xh[2 * w + 1],
-                                            smul[w], sadd[w]);
-                    *(uint4 *)(A + sd * G::A_PLANE + off) = make_uint4(wds[0], wds[1], wds[2], wds[3]);
-                }
-            }
-            if (half == 0) rowE[row] = mx == 0x7FF ? 0x7FFFFFFF : E;
-            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-            bar_arrive(bA_full);
-            if (warp == 0) {
-                // ---- MMA issue for this tile, one TMEM half at a time
-                if (!bar_wait(bA_full, it & 1)) { alive = false; break; }
-                if (it > 0 && !bar_wait(bT_empty[0], (it - 1) & 1)) { alive = false; break; }
-#pragma unroll
-                for (int i = 0; i < kM / 32; ++i)
-                    rowE_epi[(it & 1) * kM + lane + 32 * i] = rowE[lane + 32 * i];
-                __syncwarp();
-                if (lane == 0) {
-                    bar_arrive(bX_full[0]);
-                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                    issue_half<NT, 0>(tmem, a_desc0, b_desc0);
-                    commit(bT_full[0]);
-                }
-                __syncwarp();
-                if (it > 0 && !bar_wait(bT_empty[1], (it - 1) & 1)) { alive = false; break; }
-                if (lane == 0) {
-                    bar_arrive(bX_full[1]);
-                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                    issue_half<NT, 1>(tmem, a_desc0, b_desc0);
-                    commit(bT_full[1]);
-                    commit(bA_empty);
-                }
-                __syncwarp();
-            }
-        }
-    } else {
-        // ============ epilogue: warp group hf drains TMEM half hf (output blocks
-        // 2hf, 2hf+1); thread = TMEM lane = tile row; 8 outputs per step
-        const int ew = warp - kProducers / 32;
-        const int lq = ew & 3, hf = ew >> 2;
-        const int row = lq * 32 + lane;
-        double dot = 0.0;
-        uint32_t it = 0;
-        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
-            if (!bar_wait(bX_full[hf], it & 1)) { alive = false; break; }
-            const int Er = rowE_epi[(it & 1) * kM + row];
-            if (!bar_wait(bT_full[hf], it & 1)) { alive = false; break; }
-            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const int ch = (int)(tile % nch);
-            const long long lb = (tile / nch) % nlb;
-            const int arr = (int)(tile / (nch * nlb));
-            const int qc0 = S.qlo + ch * kQC;
-            const long long g = lb * kM + row;
-            const bool valid = g < nlines;
-            const long long l = valid ? g % S.nL : 0, rr = valid ? g / S.nL : 0;
-            double *__restrict__ y = S.y + (long long)arr * S.y_arr;
-            const double *__restrict__ xa = S.x + (long long)arr * S.x_arr;
-            const double *__restrict__ x2 = S.x2 ? S.x2 + (long long)arr * S.x_arr : nullptr;
-            const int se = Er + F.ef - 56;
-#pragma unroll 1
-            for (int step = 0; step < 4; ++step) {             // 2 blocks x 2 x 8 outputs
-                const int jj = step >> 1, n0 = (step & 1) * 8;
-                uint32_t acc[G::ORD][8];
-#pragma unroll
-                for (int k = 0; k < G::ORD; ++k)
-                    tmem_ld8(tmem + ((uint32_t)(lq * 32) << 16) +
-                                 (uint32_t)(hf * G::HALF_COLS + (jj * G::ORD + k) * 16 + n0),
-                             acc[k]);
-                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                if (step == 3) {                                // half drained: release it
-                    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-                    bar_arrive(bT_empty[hf]);
-                }
-                if (!valid) continue;
-                const int q0 = qc0 + 16 * (2 * hf + jj) + n0;
-                const int nv = min(8, S.qhi - q0 + 1);
-                if (nv <= 0) continue;
-                double add[8];
-#pragma unroll
-                for (int n = 0; n < 8; ++n) {
-                    add[n] = 0.0;
-                    if (x2 && n < nv) {
-                        const int q = q0 + n;
-                        const long long pos = q - S.out_lo;
-                        const long long x2i = S.bc == BC_GROW
-                            ? (S.transpose ? rr + (long long)S.nR * pos : l + (long long)S.nL * (pos + (long long)S.out_ext * rr))
-                            : l + (long long)S.nL * ((long long)(q - S.in_lo) + (long long)S.in_ext * rr);
-                        add[n] = x2[x2i];
-                    }
-                }
-#pragma unroll
-                for (int n = 0; n < 8; ++n) {
-                    if (n >= nv) break;
-                    const int q = q0 + n;
-                    // Y = sum_{k<=5} Acc_k 2^(8(5-k)) + Acc_6 2^-8 (+ Acc_7 2^-16), Horner form
-                    long long Y = __float2int_rn(__uint_as_float(acc[0][n]));
-#pragma unroll
-                    for (int k = 1; k < 6; ++k)
-                        Y = Y * 256 + __float2int_rn(__uint_as_float(acc[k][n]));
-                    int lo = __float2int_rn(__uint_as_float(acc[6][n]));
-                    if (G::ORD > 7) lo += (__float2int_rn(__uint_as_float(acc[G::ORD - 1][n])) + 128) >> 8;
-                    Y += ((long long)lo + 128) >> 8;
-                    double out = Er == 0x7FFFFFFF ? __longlong_as_double(0x7FF8000000000000LL)
-                                                  : scale_pow2(__ll2double_rn(Y), se);
-                    const long long pos = q - S.out_lo;
-                    const long long yi = S.transpose ? rr + (long long)S.nR * pos
-                                                     : l + (long long)S.nL * (pos + (long long)S.out_ext * rr);
-                    if ((S.has_dot || S.has_ax) && (S.bc != BC_GROW || (q >= 0 && q < S.n))) {
-                        const int ps = S.bc == BC_PERIODIC ? imod(q, S.n) : q - S.in_lo;
-                        const double xq = xa[l + (long long)S.nL * ((long long)ps + (long long)S.in_ext * rr)];
-                        if (S.has_dot) dot = fma(xq, out, dot);
-                        if (S.has_ax) out = fma(xq, S.a_x, out);
-                    }
-                    if (x2) out += add[n];
-                    if (S.ay_mode == 2) out += y[yi];
-                    else if (S.ay_mode == 1) out = fma(S.a_y, y[yi], out);
-                    y[yi] = out;
-                }
-            }
-        }
-        if (S.has_dot) {
-            for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
-            if (lane == 0) red[ew] = dot;
-        }
-    }
-
-    if (!alive) atomicExch(status, 1);
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
-    if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
-                     "r"(kTmemCols)
-                     : "memory");
-    if (S.has_dot && tid == 0) {
-        double sdot = 0.0;
-        for (int i = 0; i < 8; ++i) sdot += red[i];
-        S.dot_part[blockIdx.x] = sdot;
-    }
-}
-
 int g_sms[64] = {0};
+}
 
 int sm_count() {
     int dev = 0;
@@ -545,45 +25,32 @@ int sm_count() {
     return g_sms[dev];
 }
 
-long long tile_count(const Sweep &S) {
+// 128-line x qp-output-position tiles of one sweep (all narr arrays).
+long long tile_count_for(const Sweep &S, int qp) {
     const long long nlines = (long long)S.nL * S.nR;
     const long long nq = S.qhi - S.qlo + 1;
-    return ((nlines + kM - 1) / kM) * ((nq + kQC - 1) / kQC) * S.narr;
+    return ((nlines + 127) / 128) * ((nq + qp - 1) / qp) * S.narr;
 }
 
-template <int NT>
-cudaError_t launch_t(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st) {
-    using G = TcGeom<NT>;
-    static bool attr[64] = {};   // the attribute is set once per device
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64 || !attr[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(sweep_tc_kernel<NT>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM);
-        if (e != cudaSuccess) return e;
-        if (dev >= 0 && dev < 64) attr[dev] = true;
-    }
-    const long long tiles = tile_count(S);
-    const int grid = (int)(tiles < sm_count() ? tiles : sm_count());
-    sweep_tc_kernel<NT><<<grid, kThreads, G::SMEM, st>>>(S, F, status);
-    return cudaGetLastError();
-}
-
-}  // namespace
+}  // namespace tck
 
 bool sweep_tc_supported(const Sweep &S) {
-    return S.kind == KCONV && (S.ntaps == 16 || S.ntaps == 29);
+    if (S.kind == KCONV) return S.ntaps == 16 || S.ntaps == 29;
+    return (S.kind == KDEC || S.kind == KREC) && (S.ntaps == 8 || S.ntaps == 16);
 }
 
 long long sweep_tc_blocks(const Sweep &S) {
-    const long long tiles = tile_count(S);
-    return tiles < sm_count() ? tiles : sm_count();
+    const long long tiles = tck::tile_count_for(S, S.kind == KCONV ? 64 : 32);
+    const int sms = tck::sm_count();
+    return tiles < sms ? tiles : sms;
 }
 
 // Filter bytes with the operator scalar folded in exactly: a*f is formed as
 // the 106-bit product of the two mantissas, then rounded once to the 64-bit
-// fixed point |a f| 2^(64 - ef) (ef: power of two above the largest |a f|).
+// fixed point |a f| 2^(64 - ef) (ef: power of two above the largest |a f| of
+// the whole flat filter, so every channel pair shares one scale).
 void tc_filter_digits(const double *taps, int ntaps, double a, TcFilter &F) {
+    memset(&F, 0, sizeof(F));
     int ea = 0;
     const double fa = frexp(fabs(a), &ea);                          // |a| = fa 2^ea
     const unsigned long long ma = (unsigned long long)ldexp(fa, 53);  // 53-bit integer
@@ -604,8 +71,6 @@ void tc_filter_digits(const double *taps, int ntaps, double a, TcFilter &F) {
     }
     if (ef == -100000) ef = 0;
     F.ef = ef;
-    for (int s = 0; s < TcFilter::kSlices; ++s)
-        for (int i = 0; i < TcFilter::kMaxTaps; ++i) F.dig[s][i] = 0;
     for (int i = 0; i < ntaps; ++i) {
         const int sh = ep[i] + 64 - ef;                             // |F| = prod 2^sh < 2^64
         const unsigned __int128 v = prod[i];
@@ -621,9 +86,33 @@ void tc_filter_digits(const double *taps, int ntaps, double a, TcFilter &F) {
     }
 }
 
-cudaError_t launch_sweep_tc(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st) {
-    if (S.ntaps == 16) return launch_t<16>(S, F, status, st);
-    if (S.ntaps == 29) return launch_t<29>(S, F, status, st);
+// bfloat16 x 3 or tf32 x 2 terms of the FP32 value of a*f (rounded to
+// nearest); each term is its remainder rounded to nearest (ties away from
+// zero), each remainder exact in FP32 -- the split the kernel applies to x.
+void tc_filter_split(const double *taps, int ntaps, double a, int sch, TcFilter &F) {
+    memset(&F, 0, sizeof(F));
+    const int nsplit = sch == SCH_BF16X3 ? 3 : 2;
+    const uint32_t mask = sch == SCH_BF16X3 ? 0xFFFF0000u : 0xFFFFE000u;
+    const uint32_t half = (~mask + 1u) >> 1;
+    for (int i = 0; i < ntaps; ++i) {
+        float r = (float)(a * taps[i]);
+        for (int s = 0; s < nsplit; ++s) {
+            uint32_t b;
+            memcpy(&b, &r, 4);
+            const uint32_t h = (b + half) & mask;
+            float hf;
+            memcpy(&hf, &h, 4);
+            F.dig[s][i] = sch == SCH_BF16X3 ? (h >> 16) : h;
+            r = r - hf;
+        }
+    }
+}
+
+cudaError_t launch_sweep_tc(const Sweep &S, const TcFilter &F, int sch, int *status,
+                            cudaStream_t st) {
+    if (sch == SCH_EXACT) return tck::launch_exact(S, F, status, st);
+    if (sch == SCH_BF16X3) return tck::launch_bf16x3(S, F, status, st);
+    if (sch == SCH_TF32X3) return tck::launch_tf32x3(S, F, status, st);
     return cudaErrorInvalidValue;
 }
 

@@ -1,0 +1,19 @@
+// Tensor-core sweep, scheme SCH_BF16X3: convolution (16, 29 taps) and
+// wavelet decompose / recompose (8, 16 polyphase taps) instantiations.
+#include "tc_kernel.cuh"
+
+namespace lcg {
+namespace tck {
+
+cudaError_t launch_bf16x3(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st) {
+    if (S.kind == KCONV && S.ntaps == 16) return launch<KCONV, 16, SCH_BF16X3>(S, F, status, st);
+    if (S.kind == KCONV && S.ntaps == 29) return launch<KCONV, 29, SCH_BF16X3>(S, F, status, st);
+    if (S.kind == KDEC && S.ntaps == 8) return launch<KDEC, 8, SCH_BF16X3>(S, F, status, st);
+    if (S.kind == KDEC && S.ntaps == 16) return launch<KDEC, 16, SCH_BF16X3>(S, F, status, st);
+    if (S.kind == KREC && S.ntaps == 8) return launch<KREC, 8, SCH_BF16X3>(S, F, status, st);
+    if (S.kind == KREC && S.ntaps == 16) return launch<KREC, 16, SCH_BF16X3>(S, F, status, st);
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace tck
+}  // namespace lcg

@@ -45,14 +45,20 @@ extern "C" {
 #define LIBCONV_BC_GROW      1
 #define LIBCONV_BC_FREE      2
 
-/* Compute modes for libconv_gb300_set_mode (per calling thread).
- *   FP64:     plain FP64 FMA kernels on the CUDA cores (default).
- *   TC_EXACT: MagicFilter / kinetic / derivative sweeps on the tcgen05 tensor
- *             cores with exact integer digit arithmetic (FP16 digits, FP32
- *             accumulation kept exact); FP64-class accuracy. Wavelet sweeps
- *             run the FP64 kernels in this mode. */
-#define LIBCONV_MODE_FP64      0
-#define LIBCONV_MODE_TC_EXACT  1
+/* Compute modes for libconv_gb300_set_mode (per calling thread).  The
+ * tensor-core modes cover every sweep (MagicFilter, kinetic, derivative,
+ * wavelet and combined wavelet-MagicFilter filters).
+ *   FP64:      plain FP64 FMA kernels on the CUDA cores (default).
+ *   TC_EXACT:  tcgen05 tensor cores with exact integer digit arithmetic (FP16
+ *              byte digits, FP32 accumulation kept exact); FP64-class accuracy.
+ *   TC_BF16X3: split precision, 3 bfloat16 terms per operand, 6 products,
+ *              FP32 accumulation; relative error near 1e-7.
+ *   TC_TF32X3: split precision, 2 tf32 terms per operand, 3 products, FP32
+ *              accumulation; relative error near 1e-7. */
+#define LIBCONV_MODE_FP64       0
+#define LIBCONV_MODE_TC_EXACT   1
+#define LIBCONV_MODE_TC_BF16X3  2
+#define LIBCONV_MODE_TC_TF32X3  3
 
 const char *libconv_gb300_version(void);
 const char *libconv_gb300_strerror(int status);

@@ -17,7 +17,7 @@ TOL = 1e-13
 @pytest.fixture(autouse=True, params=['fp64', 'tc_exact'])
 def compute_mode(request, pkg):
     """Every parity case runs with the FP64 kernels and with the tensor-core
-    exact-digit kernels (wavelet sweeps use the FP64 kernels in both)."""
+    exact-digit kernels (every sweep kind: convolution, wavelet, combined)."""
     m = pkg.MODE_FP64 if request.param == 'fp64' else pkg.MODE_TC_EXACT
     with pkg.mode(m):
         yield request.param
