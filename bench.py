@@ -1,15 +1,27 @@
 #!/usr/bin/env python3
-"""Benchmark: FP64 3D MagicFilter + Kinetic on 128^3 periodic grids.
+"""Benchmark of the separable Daubechies-16 convolution operators.
 
-One step = the hot path over one batch of grids held in HBM: for every grid
-x of the batch, psi_r = MagicFilter3D(x) (three rotated sweeps) and
+Default workload (mfkin128): FP64 3D MagicFilter + Kinetic on 128^3 periodic
+grids.  One step = the hot path over one batch of grids held in HBM: for every
+grid x of the batch, psi_r = MagicFilter3D(x) (three rotated sweeps) and
 T x = Kinetic3D(x) (h = 0.45 bohr per axis, three accumulating sweeps), both
 from the same x.  Metric: grid points per second (points of x processed by
 both operators), whole job.  Inputs are seeded Gaussian-filtered noise
 (sigma = 2 points, unit RMS); the batch (default 32 grids, 537 MB per array)
 is larger than the 126 MB L2, so every step streams from HBM.
 
+Workload wavelet96: 3D wavelet synthesis of 8 subbands of 48^3 (coarse
+uniform [-1, 1], details uniform [-1, 1] x 1e-3) into 96^3, then analysis
+back; metric: 96^3 grid points per second through both transforms.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload mfkin128|wavelet96]
+                  [--mode tc_exact|fp64|tc_bf16x3|tc_tf32x3]
+
+Modes: tc_exact (default) runs the tensor-core exact-digit sweeps (FP64
+accuracy); fp64 the FP64 FMA sweeps; tc_bf16x3 / tc_tf32x3 the split-precision
+tensor-core sweeps, whose line carries each operator's max relative error
+against the tc_exact output of the same step.
 
 --impl reference times the CPU implementation of the same operators (the
 C oracle: a restatement of the reference's Fortran/generated loops) on all
@@ -28,25 +40,145 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-N_AXIS = 128
 HGRID = 0.45
-METRIC = 'grid pts/s, FP64 3D MagicFilter + Kinetic (128^3 periodic)'
 UNIT = 'grid pts/s'
 
 
 def peaks():
     p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
-    if os.path.exists(p):
-        d = json.load(open(p))
-        return d.get('hbm_gbs', 6800.0), 'measured'
-    return 6800.0, 'fallback'
+    d = json.load(open(p)) if os.path.exists(p) else {}
+    return {'hbm': d.get('hbm_gbs', 6800.0), 'bf16': d.get('bf16_tflops', 1900.0),
+            'source': 'measured' if d else 'fallback'}
 
 
-def base_grids(count, n):
+def package():
     import __graft_entry__ as ge
-    ge.package()
-    from boast_lig_gb300 import inputs
-    return [inputs.gaussian_filtered_noise(1000 + i, (n, n, n)).ravel(order='F') for i in range(count)]
+    return ge.package()
+
+
+# ----------------------------------------------------------------------------- workloads
+class MfKin128:
+    """MagicFilter3D + Kinetic3D on 128^3 periodic grids."""
+    name = 'mfkin128'
+    metric = 'grid pts/s, FP64 3D MagicFilter + Kinetic (128^3 periodic)'
+    n = [128, 128, 128]
+    n_in = 128 ** 3
+    n_out = 128 ** 3
+    ops = ('magicfilter3d', 'kinetic3d')
+    a = [-0.5 / HGRID ** 2] * 3
+    launches = 6                                     # 3 sweeps per operator
+    desc = ('{B} grids of 128^3 periodic per GPU per step: MagicFilter3D (d_sfrf_ld_narr) + '
+            'Kinetic3D (d_kin_narr, h=0.45)')
+
+    def base(self, count):
+        package()
+        from boast_lig_gb300 import inputs
+        return [inputs.gaussian_filtered_noise(1000 + i, tuple(self.n)).ravel(order='F')
+                for i in range(count)]
+
+    def fill(self, hx, B, rank, base):
+        N = self.n_in
+        for b in range(B):
+            hx[b * N:(b + 1) * N] = base[(b + rank) % len(base)] * (1.0 + 1e-3 * b)
+
+    def dev_ops(self, pkg, B, bufs):
+        n, a = self.n, self.a
+        mf, kin = pkg.Kernel('d_sfrf_ld_narr'), pkg.Kernel('d_kin_narr')
+        x, o0, o1, w1, w2 = bufs['x'], bufs['o0'], bufs['o1'], bufs['w1'], bufs['w2']
+        return [lambda sp: mf.run_dev(3, n, [0, 0, 0], n, n, B, x, o0, w1, w2, stream=sp),
+                lambda sp: kin.run_dev(3, n, [0, 0, 0], B, x, o1, w1, w2, a, 0.0, 0.0, stream=sp)]
+
+    def host_step(self, pkg, B, hx, ho0, ho1):
+        n, a, hw = self.n, self.a, np.zeros(1)
+        pkg.Kernel('d_sfrf_ld_narr').run(3, n, [0, 0, 0], n, n, B, hx, ho0, hw, hw)
+        pkg.Kernel('d_kin_narr').run(3, n, [0, 0, 0], B, hx, ho1, hw, hw, a, 0.0, 0.0)
+
+    e2e_note = ('d_sfrf_ld_narr (narr=B) + d_kin_narr (narr=B), host pointers (pinned), '
+                'H2D of x and D2H of psi_r and T x inside every call')
+
+    def cpu_work(self, O, x, bufs):
+        y, tx, w1, w2 = bufs
+        n = self.n
+        O.call('oracle_d_sfrf_ld_narr', 3, n, [0, 0, 0], n, n, 1, x, y, w1, w2)
+        O.call('oracle_d_kin', 3, n, [0, 0, 0], x, tx, w1, w2, np.array(self.a), 0.0, 0.0)
+
+    # roofline: dominant kernel = the kinetic sweep (29 taps), 3 launches per
+    # step over all grids; algorithmic bytes per grid point 64/3 per launch
+    # (16 B first sweep, 24 B the two accumulating sweeps)
+    dom = 1
+    dom_bytes_per_pt = 64.0 / 3.0
+    dom_flops_per_pt = 58 + 1 + 2.0 / 3.0
+    dom_kernel = {'tc_exact': 'sweep_tc_kernel<KCONV,29,EXACT> (kinetic sweep, all grids per launch)',
+                  'tc_bf16x3': 'sweep_tc_kernel<KCONV,29,BF16X3> (kinetic sweep)',
+                  'tc_tf32x3': 'sweep_tc_kernel<KCONV,29,TF32X3> (kinetic sweep)',
+                  'fp64': 'sweep_fp64_kernel<KCONV,29> (kinetic sweep, all grids per launch)'}
+    traffic_file = {'tc_exact': 'kinetic_sweep_tc_traffic.json', 'fp64': 'kinetic_sweep_fp64_traffic.json'}
+    kb = 48                                          # K per 16-output MMA block (29 taps)
+    pairs_exact = 36
+
+
+class Wavelet96:
+    """idwt 8 x 48^3 -> 96^3, then dwt back (periodic)."""
+    name = 'wavelet96'
+    metric = 'grid pts/s, 3D wavelet synthesis + analysis (8 x 48^3 <-> 96^3 periodic)'
+    n = [48, 48, 48]
+    n_in = 96 ** 3
+    n_out = 96 ** 3
+    ops = ('idwt3d', 'dwt3d')
+    launches = 6
+    desc = ('{B} grids per GPU per step: d_idwt_sym8_narr (8 subbands of 48^3 -> 96^3) then '
+            'd_dwt_sym8_narr (96^3 -> 8 x 48^3)')
+
+    def base(self, count):
+        package()
+        from boast_lig_gb300 import inputs
+        out = []
+        for i in range(count):
+            c = inputs.uniform(2000 + i, self.n_in).reshape(96, 96, 96)
+            c[48:, :, :] *= 1e-3
+            c[:, 48:, :] *= 1e-3
+            c[:, :, 48:] *= 1e-3
+            out.append(np.ascontiguousarray(c).ravel())
+        return out
+
+    fill = MfKin128.fill
+
+    def dev_ops(self, pkg, B, bufs):
+        n = self.n
+        iw, dw = pkg.Kernel('d_idwt_sym8_narr'), pkg.Kernel('d_dwt_sym8_narr')
+        x, o0, o1, w1, w2 = bufs['x'], bufs['o0'], bufs['o1'], bufs['w1'], bufs['w2']
+        return [lambda sp: iw.run_dev(3, n, [0, 0, 0], B, x, o0, w1, w2, stream=sp),
+                lambda sp: dw.run_dev(3, n, [0, 0, 0], B, o0, o1, w1, w2, stream=sp)]
+
+    def host_step(self, pkg, B, hx, ho0, ho1):
+        n, hw = self.n, np.zeros(1)
+        pkg.Kernel('d_idwt_sym8_narr').run(3, n, [0, 0, 0], B, hx, ho0, hw, hw)
+        pkg.Kernel('d_dwt_sym8_narr').run(3, n, [0, 0, 0], B, ho0, ho1, hw, hw)
+
+    e2e_note = ('d_idwt_sym8_narr then d_dwt_sym8_narr (narr=B), host pointers (pinned): '
+                'H2D of the subbands and D2H of the 96^3 grids in the first call, H2D of '
+                'the 96^3 grids and D2H of the subbands in the second')
+
+    def cpu_work(self, O, x, bufs):
+        y, back, w1, w2 = bufs
+        n = self.n
+        O.call('oracle_d_idwt_sym8', 3, n, [0, 0, 0], x, y, w1, w2)
+        O.call('oracle_d_dwt_sym8', 3, n, [0, 0, 0], y, back, w1, w2)
+
+    # roofline: every sweep moves 16 B per 96^3 point; dominant = the synthesis
+    dom = 0
+    dom_bytes_per_pt = 16.0
+    dom_flops_per_pt = 32.0
+    dom_kernel = {'tc_exact': 'sweep_tc_kernel<KREC,8,EXACT> (synthesis sweep)',
+                  'tc_bf16x3': 'sweep_tc_kernel<KREC,8,BF16X3> (synthesis sweep)',
+                  'tc_tf32x3': 'sweep_tc_kernel<KREC,8,TF32X3> (synthesis sweep)',
+                  'fp64': 'sweep_fp64_kernel<KREC,8> (synthesis sweep)'}
+    traffic_file = {}
+    kb = 32
+    pairs_exact = 28
+
+
+WORKLOADS = {'mfkin128': MfKin128(), 'wavelet96': Wavelet96()}
 
 
 class Clocks:
@@ -90,22 +222,17 @@ class Clocks:
 
 
 # ----------------------------------------------------------------------------- CPU
-def cpu_run(grids, threads, steps, warmup):
-    """Oracle MagicFilter3D + Kinetic3D, one grid per host thread (ctypes
-    releases the GIL).  Returns seconds per step (min over steps)."""
+def cpu_run(W, grids, threads, steps, warmup):
+    """The workload's oracle operators, one grid per host thread (ctypes
+    releases the GIL).  Returns the per-step times and the points per step."""
     sys.path.insert(0, os.path.join(ROOT, 'oracle'))
     import oracle as O
     O.lib()
-    n = [N_AXIS] * 3
-    N = grids[0].size
-    a = np.array([-0.5 / HGRID ** 2] * 3)
+    N = max(W.n_in, W.n_out)
     bufs = [[np.zeros(N) for _ in range(4)] for _ in range(threads)]
 
     def work(t):
-        x = grids[t % len(grids)]
-        y, tx, w1, w2 = bufs[t]
-        O.call('oracle_d_sfrf_ld_narr', 3, n, [0, 0, 0], n, n, 1, x, y, w1, w2)
-        O.call('oracle_d_kin', 3, n, [0, 0, 0], x, tx, w1, w2, a, 0.0, 0.0)
+        W.cpu_work(O, grids[t % len(grids)], bufs[t])
 
     times = []
     for s in range(warmup + steps):
@@ -118,7 +245,7 @@ def cpu_run(grids, threads, steps, warmup):
         dt = time.perf_counter() - t0
         if s >= warmup:
             times.append(dt)
-    return times, threads * N
+    return times, threads * W.n_in
 
 
 def cpu_threads():
@@ -128,33 +255,34 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def cpu_baseline_sample(grids):
-    """Bounded sample (~10 s): all host threads, one 128^3 grid each, repeated."""
+def cpu_baseline_sample(W, grids):
+    """Bounded sample (~10 s): all host threads, one grid each, repeated."""
     th = cpu_threads()
-    times, pts = cpu_run(grids, th, 1, 0)
+    times, pts = cpu_run(W, grids, th, 1, 0)
     reps = max(1, min(10, int(10.0 / max(times[0], 1e-3))))
-    times2, _ = cpu_run(grids, th, reps, 0)
+    times2, _ = cpu_run(W, grids, th, reps, 0)
     t = float(np.median(times + times2))
     return {'value': pts / t, 'unit': UNIT, 'cores': th, 'kind': 'port',
-            'sample': f'{th} grids of 128^3 (one per thread) x {1 + reps} repetitions, '
-                      f'MagicFilter3D + Kinetic3D, C oracle, median step {t:.3f} s'}
+            'sample': f'{th} grids (one per thread) x {1 + reps} repetitions of the '
+                      f'{W.name} operators, C oracle, median step {t:.3f} s'}
 
 
 def run_reference(args):
     rank = int(os.environ.get('RANK', '0'))
     if rank != 0:
         return
-    grids = base_grids(4, N_AXIS)
+    W = WORKLOADS[args.workload]
+    grids = W.base(4)
     th = cpu_threads()
-    times, pts = cpu_run(grids, th, args.steps, max(args.warmup, 1))
+    times, pts = cpu_run(W, grids, th, args.steps, max(args.warmup, 1))
     t = float(np.median(times))
     v = pts / t
-    line = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': UNIT, 'n_gpus': args.gpus,
-            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': t * 1e3,
-            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
-            'data': 'synthetic (seeded Gaussian-filtered noise)',
-            'config': {'workload': f'{th} grids of 128^3 periodic per step, one per host thread, '
-                                   'MagicFilter3D + Kinetic3D (h=0.45)', 'grid': [128, 128, 128]},
+    line = {'impl': 'reference', 'metric': W.metric, 'value': v, 'unit': UNIT,
+            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': t * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded)',
+            'config': {'workload': f'{th} grids per step, one per host thread, {W.name} '
+                                   'operators', 'grid': W.n},
             'cpu_baseline': {'value': v, 'unit': UNIT, 'cores': th, 'kind': 'port',
                              'sample': f'{args.steps} steps of {th} grids (one per thread), '
                                        'C oracle restating the reference loops'},
@@ -163,10 +291,14 @@ def run_reference(args):
 
 
 # ----------------------------------------------------------------------------- GPU
+MODES = {'fp64': 'MODE_FP64', 'tc_exact': 'MODE_TC_EXACT', 'tc_bf16x3': 'MODE_TC_BF16X3',
+         'tc_tf32x3': 'MODE_TC_TF32X3'}
+
+
 def run_gpu(args):
     import torch
-    import __graft_entry__ as ge
-    pkg = ge.package()
+    pkg = package()
+    W = WORKLOADS[args.workload]
     world = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
     local = int(os.environ.get('LOCAL_RANK', '0'))
@@ -176,40 +308,31 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group('nccl', device_id=dev)
     B = args.grids
-    n = [N_AXIS] * 3
-    N = N_AXIS ** 3
-    base = base_grids(4, N_AXIS)
-    host_x = torch.empty(B * N, dtype=torch.float64, pin_memory=True)
+    Ni, No = W.n_in, W.n_out
+    base = W.base(4)
+    host_x = torch.empty(B * Ni, dtype=torch.float64, pin_memory=True)
     hx = host_x.numpy()
-    for b in range(B):
-        hx[b * N:(b + 1) * N] = base[(b + rank) % 4] * (1.0 + 1e-3 * b)
-    xd = host_x.to(dev)
-    psir = torch.empty(B * N, dtype=torch.float64, device=dev)
-    tx = torch.empty(B * N, dtype=torch.float64, device=dev)
-    w1 = torch.empty(B * N, dtype=torch.float64, device=dev)
-    w2 = torch.empty(B * N, dtype=torch.float64, device=dev)
-    a = [-0.5 / HGRID ** 2] * 3
-    tc = args.mode == 'tc_exact'
-    pkg.set_mode(pkg.MODE_TC_EXACT if tc else pkg.MODE_FP64)
-    mf = pkg.Kernel('d_sfrf_ld_narr')
-    kin = pkg.Kernel('d_kin_narr')
+    W.fill(hx, B, rank, base)
+    bufs = {'x': host_x.to(dev)}
+    for k in ('o0', 'o1', 'w1', 'w2'):
+        bufs[k] = torch.empty(B * max(Ni, No), dtype=torch.float64, device=dev)
+    pkg.set_mode(getattr(pkg, MODES[args.mode]))
+    ops = W.dev_ops(pkg, B, bufs)
     stream = torch.cuda.Stream(device=dev)
     sp = stream.cuda_stream
-    base_ptr = xd.data_ptr()
 
     def step(evs=None):
+        for i, op in enumerate(ops):
+            if evs:
+                evs[i].record(stream)
+            op(sp)
         if evs:
-            evs[0].record(stream)
-        mf.run_dev(3, n, [0, 0, 0], n, n, B, xd, psir, w1, w2, stream=sp)
-        if evs:
-            evs[1].record(stream)
-        kin.run_dev(3, n, [0, 0, 0], B, xd, tx, w1, w2, a, 0.0, 0.0, stream=sp)
-        if evs:
-            evs[2].record(stream)
+            evs[len(ops)].record(stream)
 
     for _ in range(max(args.warmup, 3)):
         step()
     stream.synchronize()
+    pkg.check(sp)
 
     def barrier():
         if world > 1:
@@ -217,7 +340,8 @@ def run_gpu(args):
             dist.barrier()
 
     clocks = Clocks(local)
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(len(ops) + 1)]
+           for _ in range(args.steps)]
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     torch.cuda.synchronize()
@@ -230,82 +354,95 @@ def run_gpu(args):
     torch.cuda.synchronize()
     barrier()
     ck = clocks.stop()
+    pkg.check(sp)
     ms = start.elapsed_time(stop)
-    mf_ms = sum(e[0].elapsed_time(e[1]) for e in evs)
-    kin_ms = sum(e[1].elapsed_time(e[2]) for e in evs)
+    op_ms = [sum(e[i].elapsed_time(e[i + 1]) for e in evs) for i in range(len(ops))]
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = t.item()
-    pts_step = B * N * world
+    pts_step = B * Ni * world
     value = pts_step * args.steps / (ms / 1e3)
 
+    # split precision: each operator's max relative error against the
+    # exact-digit (FP64-accurate) output of the same step
+    accuracy = None
+    if args.mode in ('tc_bf16x3', 'tc_tf32x3'):
+        got = [bufs['o0'][:B * No].clone(), bufs['o1'][:B * No].clone()]
+        pkg.set_mode(pkg.MODE_TC_EXACT)
+        step()
+        stream.synchronize()
+        ref = [bufs['o0'][:B * No], bufs['o1'][:B * No]]
+        accuracy = {'reference': 'tc_exact output of the same step (FP64-accurate)'}
+        for name, g, r in zip(W.ops, got, ref):
+            accuracy[name] = float((g - r).abs().max() / r.abs().max())
+        pkg.set_mode(getattr(pkg, MODES[args.mode]))
+
     # e2e: the public host-pointer C-ABI with pinned host buffers, copies inside
-    host_psir = torch.empty(B * N, dtype=torch.float64, pin_memory=True).numpy()
-    host_tx = torch.empty(B * N, dtype=torch.float64, pin_memory=True).numpy()
-    hw = np.zeros(1)
-
-    def e2e_step():
-        mf.run(3, n, [0, 0, 0], n, n, B, hx, host_psir, hw, hw)
-        kin.run(3, n, [0, 0, 0], B, hx, host_tx, hw, hw, a, 0.0, 0.0)
-
-    e2e_step()
+    ho0 = torch.empty(B * max(Ni, No), dtype=torch.float64, pin_memory=True).numpy()
+    ho1 = torch.empty(B * max(Ni, No), dtype=torch.float64, pin_memory=True).numpy()
+    W.host_step(pkg, B, hx, ho0, ho1)
     barrier()
     e_steps = max(2, min(args.steps, 5))
     t0 = time.perf_counter()
     for _ in range(e_steps):
-        e2e_step()
+        W.host_step(pkg, B, hx, ho0, ho1)
     torch.cuda.synchronize()
     barrier()
     e_t = (time.perf_counter() - t0) / e_steps
-    e2e = {'value': pts_step / e_t, 'unit': UNIT, 'h2d_bytes_per_step': 2 * B * N * 8,
-           'd2h_bytes_per_step': 2 * B * N * 8,
-           'note': 'd_sfrf_ld_narr (narr=B) + d_kin_narr (narr=B), host pointers (pinned), '
-                   'H2D of x and D2H of psi_r and T x inside every call'}
-
-    # roofline of the dominant kernel (kinetic sweep, 29 taps): 3 launches per
-    # grid; algorithmic bytes per grid 64 B/pt (16 + 24 + 24)
-    hbm, src = peaks()
-    launches_kin = 3 * args.steps
-    t_launch = kin_ms / 1e3 / launches_kin
-    bytes_launch = 64.0 / 3.0 * N * B
-    achieved = bytes_launch / t_launch / 1e9
-    flops_launch = (58 + 1 + 2.0 / 3.0) * N * B  # 29 FMA, scale, x2 add (2 of 3 sweeps)
-    traffic = None
-    kname = ('sweep_tc_kernel<29> (kinetic sweep, all grids per launch)' if tc
-             else 'sweep_fp64_kernel<KCONV,29> (kinetic sweep, all grids per launch)')
-    tp = os.path.join(ROOT, 'profiles', ('kinetic_sweep_tc_traffic.json' if tc
-                                         else 'kinetic_sweep_fp64_traffic.json'))
-    if os.path.exists(tp):
-        tj = json.load(open(tp))
-        traffic = tj['dram_bytes_per_point'] * N * B
-    roof = {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
-            'frac': achieved / hbm, 'traffic': traffic, 'kernel': kname, 'peak_source': src}
-    if tc:
-        # tensor work per output: 28 digit pairs x K=48 x 2 flops (not algorithmic flops)
-        bf = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))).get('bf16_tflops', 1900.0) \
-            if os.path.exists(os.path.join(ROOT, 'MEASURED_PEAKS.json')) else 1900.0
-        tflops = 36 * 48 * 2 * N * B / t_launch / 1e12
-        roof['tensor_pipe'] = {'mma_tflops': tflops, 'peak_tflops': bf, 'frac': tflops / bf,
-                               'note': 'exact FP16-digit MMAs (36 byte pairs, K=48 per 16 outputs)'}
+    if W.name == 'mfkin128':
+        h2d, d2h = 2 * B * Ni * 8, 2 * B * No * 8
     else:
-        roof['fp64_pipe'] = {'achieved_tflops': flops_launch / t_launch / 1e12,
+        h2d, d2h = B * (Ni + No) * 8, B * (Ni + No) * 8
+    e2e = {'value': pts_step / e_t, 'unit': UNIT, 'h2d_bytes_per_step': h2d,
+           'd2h_bytes_per_step': d2h, 'note': W.e2e_note}
+
+    # roofline of the dominant kernel
+    pk = peaks()
+    launches_dom = 3 * args.steps
+    t_launch = op_ms[W.dom] / 1e3 / launches_dom
+    pts_launch = Ni * B
+    achieved = W.dom_bytes_per_pt * pts_launch / t_launch / 1e9
+    traffic = None
+    tf = W.traffic_file.get(args.mode)
+    if tf and os.path.exists(os.path.join(ROOT, 'profiles', tf)):
+        tj = json.load(open(os.path.join(ROOT, 'profiles', tf)))
+        traffic = tj['dram_bytes_per_point'] * pts_launch
+    roof = {'bound': 'hbm', 'achieved': achieved, 'peak': pk['hbm'], 'unit': 'GB/s',
+            'frac': achieved / pk['hbm'], 'traffic': traffic, 'kernel': W.dom_kernel[args.mode],
+            'peak_source': pk['source'],
+            'algorithmic_bytes_per_point': W.dom_bytes_per_pt}
+    if args.mode != 'fp64':
+        # MMA work per output point (not algorithmic flops): products x K x 2
+        prods = {'tc_exact': W.pairs_exact, 'tc_bf16x3': 6, 'tc_tf32x3': 3}[args.mode]
+        mma_tflops = prods * W.kb * 2 * pts_launch / t_launch / 1e12
+        peak_t = pk['bf16'] / (2 if args.mode == 'tc_tf32x3' else 1)
+        roof['tensor_pipe'] = {'mma_tflops': mma_tflops, 'peak_tflops': peak_t,
+                               'frac': mma_tflops / peak_t,
+                               'note': f'{prods} operand-plane products, K={W.kb} per 16 outputs'
+                                       + ('; tf32 peak = half the measured bf16 peak'
+                                          if args.mode == 'tc_tf32x3' else '')}
+    else:
+        roof['fp64_pipe'] = {'achieved_tflops': W.dom_flops_per_pt * pts_launch / t_launch / 1e12,
                              'nominal_peak_tflops': 1.25,
                              'note': 'plain FP64 FMA path: bound by the FP64 pipe, not HBM'}
-    line = {'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+    exact = args.mode in ('fp64', 'tc_exact')
+    line = {'metric': W.metric, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
             'warmup': max(args.warmup, 3), 'ms_per_step': ms / args.steps, 'higher_is_better': True,
-            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
-            'data': 'synthetic (seeded Gaussian-filtered noise, sigma=2, unit RMS)',
-            'config': {'workload': f'{B} grids of 128^3 periodic per GPU per step: '
-                                   'MagicFilter3D (d_sfrf_ld_narr) + Kinetic3D (d_kin_narr, h=0.45)',
-                       'grid': n, 'grids_per_gpu': B, 'mode': args.mode,
-                       'l2': 'inputs larger than L2 (537 MB per array)',
-                       'ms_magicfilter3d': mf_ms / args.steps, 'ms_kinetic3d': kin_ms / args.steps},
-            'clocks': ck, 'e2e': e2e, 'gpu_launches': args.steps * 6,
+            'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f64' if exact else ('f64 in HBM, ' + args.mode[3:] + ' split on tensor cores'),
+            'data': 'synthetic (seeded)',
+            'config': {'workload': W.desc.format(B=B), 'grid': W.n, 'grids_per_gpu': B,
+                       'mode': args.mode,
+                       'l2': f'inputs larger than L2 ({B * Ni * 8 / 1e6:.0f} MB per array)',
+                       **{f'ms_{o}': t / args.steps for o, t in zip(W.ops, op_ms)}},
+            'clocks': ck, 'e2e': e2e, 'gpu_launches': args.steps * W.launches,
             'roofline': roof}
+    if accuracy:
+        line['accuracy_max_rel_error'] = accuracy
     if rank == 0 and world == 1 and not args.no_cpu:
-        line['cpu_baseline'] = cpu_baseline_sample(base)
+        line['cpu_baseline'] = cpu_baseline_sample(W, base)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -319,10 +456,12 @@ def main():
     ap.add_argument('--steps', type=int, default=10)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--workload', default='mfkin128', choices=list(WORKLOADS))
     ap.add_argument('--grids', type=int, default=32)
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline sample')
-    ap.add_argument('--mode', default='tc_exact', choices=['tc_exact', 'fp64'],
-                    help='tc_exact: tensor-core exact-digit sweeps (FP64-accurate); fp64: FP64 FMA')
+    ap.add_argument('--mode', default='tc_exact', choices=list(MODES),
+                    help='tc_exact: tensor-core exact-digit sweeps (FP64-accurate); fp64: FP64 '
+                         'FMA; tc_bf16x3 / tc_tf32x3: split precision (error reported)')
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)

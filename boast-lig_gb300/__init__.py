@@ -41,6 +41,7 @@ _MDT = [_int, _I, _I, _I, _I, _int, _vp, _vp, _vp, _vp]
 _WMD = [_int, _I, _I, _vp, _vp, _vp, _vp]
 _KIN = [_int, _I, _I, _vp, _vp, _vp, _vp, _D, _dbl, _dbl]
 _KINN = [_int, _I, _I, _int, _vp, _vp, _vp, _vp, _D, _dbl, _dbl]
+_WMDN = [_int, _I, _I, _int, _vp, _vp, _vp, _vp]
 
 SIGNATURES = {
     'd_s0s0_1d_sym8_md': _CONV1D, 'd_s0s0_1d_sym8_imd': _CONV1D, 'd_s0s0_1d_sym8_d1': _CONV1D,
@@ -49,6 +50,7 @@ SIGNATURES = {
     'd_s0s1_1d_symicomb8': _WAV1D, 'd_s1s0_1d_symicomb8': _WAV1D,
     'd_sfrf_ld_narr': _MDT, 'd_rfsf_ld_narr': _MDT,
     'd_kin': _KIN, 'd_kin_narr': _KINN, 'd_dwt_sym8': _WMD, 'd_idwt_sym8': _WMD,
+    'd_dwt_sym8_narr': _WMDN, 'd_idwt_sym8_narr': _WMDN,
 }
 COST_SIGNATURES = {
     'd_s0s0_1d_sym8_md_cost': [_int, _int, _I, _int, _int, _L],

@@ -632,6 +632,33 @@ int d_idwt_sym8_dev(int d, const int *n, const int *bc, const double *x, double 
     return rc ? rc : exec_dev(P, x, y, w1, w2, nullptr, stream);
 }
 
+int d_dwt_sym8_narr(int d, const int *n, const int *bc, int narr, const double *x, double *y,
+                    double *w1, double *w2) {
+    (void)w1; (void)w2;
+    Plan P;
+    int rc = plan_md_t(OP_DWT, d, n, bc, nullptr, nullptr, narr, P);
+    return rc ? rc : exec_host(P, x, y, nullptr);
+}
+int d_idwt_sym8_narr(int d, const int *n, const int *bc, int narr, const double *x, double *y,
+                     double *w1, double *w2) {
+    (void)w1; (void)w2;
+    Plan P;
+    int rc = plan_md_t(OP_IWT, d, n, bc, nullptr, nullptr, narr, P);
+    return rc ? rc : exec_host(P, x, y, nullptr);
+}
+int d_dwt_sym8_narr_dev(int d, const int *n, const int *bc, int narr, const double *x,
+                        double *y, double *w1, double *w2, void *stream) {
+    Plan P;
+    int rc = plan_md_t(OP_DWT, d, n, bc, nullptr, nullptr, narr, P);
+    return rc ? rc : exec_dev(P, x, y, w1, w2, nullptr, stream);
+}
+int d_idwt_sym8_narr_dev(int d, const int *n, const int *bc, int narr, const double *x,
+                         double *y, double *w1, double *w2, void *stream) {
+    Plan P;
+    int rc = plan_md_t(OP_IWT, d, n, bc, nullptr, nullptr, narr, P);
+    return rc ? rc : exec_dev(P, x, y, w1, w2, nullptr, stream);
+}
+
 int d_kin(int d, const int *n, const int *bc, const double *x, double *y, double *w1, double *w2,
           const double *a, double a_x, double a_y) {
     (void)w1; (void)w2;

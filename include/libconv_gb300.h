@@ -188,6 +188,13 @@ int d_dwt_sym8(int d, const int *n, const int *bc, const double *x, double *y, d
                double *w2);
 int d_idwt_sym8(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
                 double *w2);
+/* Extension (no counterpart in the generated code): the same 3D wavelet
+ * analysis / synthesis over narr grids laid back to back, one launch per
+ * sweep. */
+int d_dwt_sym8_narr(int d, const int *n, const int *bc, int narr, const double *x, double *y,
+                    double *w1, double *w2);
+int d_idwt_sym8_narr(int d, const int *n, const int *bc, int narr, const double *x, double *y,
+                     double *w1, double *w2);
 
 /* Device-pointer forms; w1/w2 are device workspaces sized like the
  * reference's (the largest intermediate grid, times narr). */
@@ -203,6 +210,10 @@ int d_kin_narr_dev(int d, const int *n, const int *bc, int narr, const double *x
                    double *w1, double *w2, const double *a, double a_x, double a_y, void *stream);
 int d_dwt_sym8_dev(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
                    double *w2, void *stream);
+int d_dwt_sym8_narr_dev(int d, const int *n, const int *bc, int narr, const double *x,
+                        double *y, double *w1, double *w2, void *stream);
+int d_idwt_sym8_narr_dev(int d, const int *n, const int *bc, int narr, const double *x,
+                         double *y, double *w1, double *w2, void *stream);
 int d_idwt_sym8_dev(int d, const int *n, const int *bc, const double *x, double *y,
                     double *w1, double *w2, void *stream);
 

@@ -305,3 +305,25 @@ def test_kinetic3d_narr_extension(pkg, O):
         assert O.call('oracle_d_kin', 3, n, [0, 0, 0], x[j * N:(j + 1) * N].copy(), yo,
                       np.zeros(N), np.zeros(N), np.array(a), 0.25, 0.5) == 0
         assert rel(yg[j * N:(j + 1) * N], yo) <= TOL
+
+
+@pytest.mark.parametrize('bcs', [[0, 0, 0], [1, 1, 1], [-1, -1, -1], [2, 2, 2]])
+def test_wavelet3d_narr_extension(pkg, O, bcs):
+    """d_dwt_sym8_narr / d_idwt_sym8_narr: narr grids in one call equal the
+    oracle's d_dwt_sym8 / d_idwt_sym8 on each grid."""
+    n = [6, 5, 7]
+    m = [2 * v + 14 if b == -1 else 2 * v for v, b in zip(n, bcs)]
+    mo = [2 * v + 14 if b == 1 else 2 * v for v, b in zip(n, bcs)]
+    Ni, No = int(np.prod(m)), int(np.prod(mo))
+    big = int(np.prod([max(a, b) for a, b in zip(m, mo)]))
+    narr = 3
+    x = seeded(32, Ni * narr)
+    for op in ('d_dwt_sym8', 'd_idwt_sym8'):
+        yg = np.zeros(No * narr)
+        w = np.zeros(1)
+        pkg.Kernel(op + '_narr').run(3, n, bcs, narr, x, yg, w, w)
+        for j in range(narr):
+            yo = np.zeros(No)
+            assert O.call('oracle_' + op, 3, n, bcs, x[j * Ni:(j + 1) * Ni].copy(), yo,
+                          np.zeros(big), np.zeros(big)) == 0
+            assert rel(yg[j * No:(j + 1) * No], yo) <= TOL, (op, j)
