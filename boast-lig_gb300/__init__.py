@@ -243,3 +243,101 @@ def cost(name, *args):
     if st:
         raise LibconvError(st, name, last_error())
     return out.value
+
+
+# ---- batched operators over many uneven grids ------------------------------------
+BATCH_OP_MF, BATCH_OP_KIN = 0, 1
+ENGINE_FP64_Q64, ENGINE_FP64_Q32, ENGINE_TC = 0, 1, 2
+
+
+def _stream_ptr(stream):
+    s = stream
+    if s is not None and not isinstance(s, int):
+        s = s.cuda_stream if hasattr(s, 'cuda_stream') else int(s)
+    return ctypes.c_void_p(s) if s else None
+
+
+def _batch_lib():
+    L = lib()
+    if not getattr(L, '_batch_bound', False):
+        P = ctypes.POINTER(ctypes.c_void_p)
+        L.libconv_batch_create.argtypes = [P, _int, _I, _I, _I, _D, _dbl]
+        L.libconv_batch_sizes.argtypes = [_vp, _L, _L, _L]
+        L.libconv_batch_offsets.argtypes = [_vp, _L, _L, _L]
+        L.libconv_batch_set_config.argtypes = [_vp, _int, _int, _I]
+        L.libconv_batch_get_config.argtypes = [_vp, _int, _I, _I, _I]
+        L.libconv_batch_tune.argtypes = [_vp, _vp, _vp, _vp, _vp]
+        L.libconv_batch_run.argtypes = [_vp, _vp, _vp, _vp, _vp]
+        L.libconv_batch_destroy.argtypes = [_vp]
+        for n in ('create', 'sizes', 'offsets', 'set_config', 'get_config', 'tune', 'run', 'destroy'):
+            getattr(L, 'libconv_batch_' + n).restype = _int
+        L._batch_bound = True
+    return L
+
+
+class Batch:
+    """MagicFilter3D and/or Kinetic3D over many grids of different sizes in
+    one persistent launch per sweep stage, replayed as a CUDA graph
+    (``libconv_batch_*``).  Buffers are packed float64 CUDA tensors."""
+
+    def __init__(self, dims, mf_bc=None, kin_bc=None, kin_a=None, kin_ax=0.0):
+        L = _batch_lib()
+        dims = [int(v) for d in dims for v in d]
+        self.ngrids = len(dims) // 3
+        self._h = ctypes.c_void_p()
+        a = None
+        if kin_a is not None:
+            a = ctypes.cast((ctypes.c_double * 3)(*[float(v) for v in kin_a]), _D)
+        st = L.libconv_batch_create(ctypes.byref(self._h), self.ngrids, _ints(dims), _ints(mf_bc),
+                                    _ints(kin_bc), a, float(kin_ax))
+        if st:
+            raise LibconvError(st, 'libconv_batch_create', last_error())
+
+    def _check(self, st, name):
+        if st:
+            raise LibconvError(st, name, last_error())
+
+    def sizes(self):
+        v = [ctypes.c_longlong() for _ in range(3)]
+        self._check(_batch_lib().libconv_batch_sizes(self._h, *[ctypes.byref(t) for t in v]),
+                    'libconv_batch_sizes')
+        return tuple(t.value for t in v)
+
+    def offsets(self):
+        arrs = [(ctypes.c_longlong * (self.ngrids + 1))() for _ in range(3)]
+        self._check(_batch_lib().libconv_batch_offsets(self._h, *[ctypes.cast(a, _L) for a in arrs]),
+                    'libconv_batch_offsets')
+        return tuple(list(a) for a in arrs)
+
+    def set_config(self, op, engine, order):
+        self._check(_batch_lib().libconv_batch_set_config(self._h, op, engine, _ints(order)),
+                    'libconv_batch_set_config')
+
+    def get_config(self, op):
+        e, t = ctypes.c_int(), ctypes.c_int()
+        o = (ctypes.c_int * 3)()
+        self._check(_batch_lib().libconv_batch_get_config(self._h, op, ctypes.byref(e),
+                                                          ctypes.cast(o, _I), ctypes.byref(t)),
+                    'libconv_batch_get_config')
+        return e.value, list(o), bool(t.value)
+
+    def tune(self, x, y_mf=None, y_kin=None, stream=None):
+        self._check(_batch_lib().libconv_batch_tune(self._h, _dev_ptr(x), _dev_ptr(y_mf),
+                                                    _dev_ptr(y_kin), _stream_ptr(stream)),
+                    'libconv_batch_tune')
+
+    def run(self, x, y_mf=None, y_kin=None, stream=None):
+        self._check(_batch_lib().libconv_batch_run(self._h, _dev_ptr(x), _dev_ptr(y_mf),
+                                                   _dev_ptr(y_kin), _stream_ptr(stream)),
+                    'libconv_batch_run')
+
+    def close(self):
+        if self._h:
+            _batch_lib().libconv_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

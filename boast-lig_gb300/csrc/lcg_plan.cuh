@@ -1,0 +1,41 @@
+// Plans: the sequence of 1D sweeps one entry point runs, with the buffers
+// (x, y, w1, w2) each sweep reads and writes.  Shared by the C-ABI entry
+// points and the batched (many-grid) operators.
+#pragma once
+#include <vector>
+
+#include "lcg_sweep.cuh"
+
+namespace lcg {
+
+enum BufId { B_X = 0, B_Y = 1, B_W1 = 2, B_W2 = 3 };
+
+struct PlanStep {
+    Sweep S;
+    int src, dst, src2;   // buffer ids (src2 = -1 if no x2)
+};
+
+struct Plan {
+    std::vector<PlanStep> steps;
+    size_t elems[4] = {0, 0, 0, 0};   // elements each buffer must hold
+    size_t y_read = 0;                // y is read (a_y != 0)
+    int has_dot = 0;
+};
+
+// 3D MagicFilter (sfrf_ld_narr, one grid).  order == nullptr: the reference's
+// rotating sweeps (transpose = 1); otherwise non-rotating sweeps along
+// axes order[0], order[1], order[2] (same result, other intermediates).
+int plan_magicfilter(int d, const int *n, const int *bc, const int *order, Plan &P);
+// 3D kinetic (one grid), sweeps along order[] (nullptr: 0, 1, ..., d-1).
+int plan_kinetic(int d, const int *n, const int *bc, const double *a, double a_x,
+                 const int *order, Plan &P);
+// Host copy of the flat filter table.
+const double *filter_table();
+// Calling thread's compute mode (LIBCONV_MODE_*).
+int current_mode();
+// Device status word of the current device (bounded tensor-core waits).
+int *device_status(int &rc);
+int report(int code, const char *msg);
+int report_cuda(cudaError_t e, const char *what);
+
+}  // namespace lcg

@@ -36,6 +36,16 @@ struct Sweep {
 long long sweep_fp64_blocks(const Sweep &S);
 // Enqueue the FP64 SIMT sweep on `st`.
 cudaError_t launch_sweep_fp64(const Sweep &S, cudaStream_t st);
+// Blocks of S in the batched FP64 sweep with output chunk qc (64 or 32;
+// halved for the two-channel wavelet sweeps).
+long long sweep_fp64_batch_blocks(const Sweep &S, int qc);
+// Persistent grid of the batched FP64 sweep (SMs x resident CTAs per SM).
+int sweep_fp64_batch_grid(int kind, int ntaps, int qc);
+// One persistent launch over nsweeps sweeps (device descriptors, block
+// prefix sums with prefix[nsweeps] = total) of one kind and filter; no dot.
+cudaError_t launch_sweep_fp64_batch(int kind, int ntaps, int qc, const Sweep *descs,
+                                    const long long *prefix, int nsweeps, int grid,
+                                    cudaStream_t st);
 // Deterministic sum of `count` partials into *out (device), on `st`.
 cudaError_t launch_dot_reduce(const double *part, long long count, double *out, int accumulate,
                               cudaStream_t st);

@@ -31,6 +31,14 @@ long long sweep_tc_blocks(const Sweep &S);
 // status (device int) is set non-zero if a tensor-core wait timed out.
 cudaError_t launch_sweep_tc(const Sweep &S, const TcFilter &F, int sch, int *status,
                             cudaStream_t st);
+// Tiles of one sweep (the unit a batched launch numbers consecutively).
+long long sweep_tc_tiles(const Sweep &S);
+bool sweep_tc_batch_supported(int kind, int ntaps);
+// One persistent launch over nsweeps sweeps (device descriptor array, tile
+// prefix sums with prefix[nsweeps] = total) of one kind and filter.
+cudaError_t launch_sweep_tc_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
+                                  int nsweeps, const TcFilter &F, int sch, int *status,
+                                  cudaStream_t st);
 
 namespace tck {
 long long tile_count_for(const Sweep &S, int qp);
@@ -39,6 +47,12 @@ int sm_count();
 cudaError_t launch_exact(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st);
 cudaError_t launch_bf16x3(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st);
 cudaError_t launch_tf32x3(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st);
+cudaError_t launch_exact_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
+                               int nsweeps, const TcFilter &F, int *status, cudaStream_t st);
+cudaError_t launch_bf16x3_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
+                                int nsweeps, const TcFilter &F, int *status, cudaStream_t st);
+cudaError_t launch_tf32x3_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
+                                int nsweeps, const TcFilter &F, int *status, cudaStream_t st);
 }  // namespace tck
 
 }  // namespace lcg

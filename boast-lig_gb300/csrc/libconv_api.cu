@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/libconv_gb300.h"
+#include "lcg_plan.cuh"
 #include "lcg_sweep.cuh"
 #include "lcg_tc.cuh"
 #include "libconv_filters.h"
@@ -160,20 +161,6 @@ DevState *dev_state(int &rc) {
 }
 
 // ---- plans -------------------------------------------------------------------
-enum BufId { B_X = 0, B_Y = 1, B_W1 = 2, B_W2 = 3 };
-
-struct PlanStep {
-    Sweep S;
-    int src, dst, src2;   // buffer ids (src2 = -1 if no x2)
-};
-
-struct Plan {
-    std::vector<PlanStep> steps;
-    size_t elems[4] = {0, 0, 0, 0};   // elements each buffer must hold
-    size_t y_read = 0;                // y is read (a_y != 0)
-    int has_dot = 0;
-};
-
 void need(Plan &P, int b, size_t e) { if (P.elems[b] < e) P.elems[b] = e; }
 
 // 1D dispatcher (GenericConvolution2.rb:1560-1764).
@@ -273,10 +260,50 @@ int plan_md_t(const OpDef &op, int d, const int *n, const int *bc, const int *nx
     return LIBCONV_OK;
 }
 
+// Multi-D, transpose = 0, sweeps along order[0..d-1]: the same operator as
+// plan_md_t (each sweep maps one axis in place instead of rotating it to the
+// end, so after d sweeps both give the natural axis order), other
+// intermediate shapes.
+int plan_md_n(const OpDef &op, int d, const int *n, const int *bc, const int *order, Plan &P) {
+    if (d < 1 || d > 16) return fail(LIBCONV_EARG, "d=%d out of [1,16]", d);
+    if (!n || !bc || !order) return fail(LIBCONV_EARG, "n/bc/order must not be null");
+    const long long m = nch(op);
+    long long dims[16];
+    unsigned seen = 0;
+    for (int i = 0; i < d; ++i) {
+        if (n[i] < 1) return fail(LIBCONV_EARG, "n[%d]=%d", i, n[i]);
+        if (!bc_valid(bc[i])) return fail(LIBCONV_EBC, "unknown boundary condition %d", bc[i]);
+        if (order[i] < 0 || order[i] >= d || (seen >> order[i]) & 1u)
+            return fail(LIBCONV_EARG, "sweep order is not a permutation of 0..%d", d - 1);
+        seen |= 1u << order[i];
+        dims[i] = need_in(op, bc[i], n[i]) * m;
+    }
+    for (int k = 0; k < d; ++k) {
+        const int i = order[k];
+        long long nL = 1, nR = 1;
+        for (int j = 0; j < i; ++j) nL *= dims[j];
+        for (int j = i + 1; j < d; ++j) nR *= dims[j];
+        if (nL * nR > (1LL << 31) - 1) return fail(LIBCONV_EARG, "too many lines");
+        const int in_ext = (int)(dims[i] / m);
+        const int out_ext = need_out(op, bc[i], n[i]);
+        PlanStep st;
+        geometry(op, bc[i], (int)nL, n[i], (int)nR, in_ext, out_ext, st.S);
+        st.S.x_arr = nL * nR * dims[i];
+        st.S.y_arr = nL * nR * out_ext * m;
+        pingpong(d, k, st.src, st.dst);
+        st.src2 = -1;
+        need(P, st.src, st.S.x_arr);
+        need(P, st.dst, st.S.y_arr);
+        P.steps.push_back(st);
+        dims[i] = out_ext * m;
+    }
+    return LIBCONV_OK;
+}
+
 // Multi-D kinetic, transpose = 0 (Kinetic2.rb:1068-1090), over narr grids
 // laid back to back (narr = 1 is the reference's Kinetic()).
 int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, double a_y,
-             Plan &P, int narr = 1) {
+             Plan &P, int narr = 1, const int *order = nullptr) {
     if (narr < 1 || narr > 65535) return fail(LIBCONV_EARG, "narr=%d out of [1,65535]", narr);
     if (d < 1 || d > 16) return fail(LIBCONV_EARG, "d=%d out of [1,16]", d);
     if (!n || !bc || !a) return fail(LIBCONV_EARG, "n/bc/a must not be null");
@@ -289,24 +316,33 @@ int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, do
         tot *= n[i];
     }
     if (tot > (1LL << 31) - 1) return fail(LIBCONV_EARG, "grid too large");
-    for (int i = 0; i < d; ++i) {
+    if (order) {
+        unsigned seen = 0;
+        for (int k = 0; k < d; ++k) {
+            if (order[k] < 0 || order[k] >= d || (seen >> order[k]) & 1u)
+                return fail(LIBCONV_EARG, "sweep order is not a permutation of 0..%d", d - 1);
+            seen |= 1u << order[k];
+        }
+    }
+    for (int k = 0; k < d; ++k) {
+        const int i = order ? order[k] : k;
         long long nL = 1, nR = 1;
         for (int j = 0; j < i; ++j) nL *= n[j];
         for (int j = i + 1; j < d; ++j) nR *= n[j];
         PlanStep st;
         geometry(OP_D2, bc[i], (int)nL, n[i], (int)nR, n[i], n[i], st.S);
-        const bool last = i == d - 1;
+        const bool last = k == d - 1;
         st.S.has_a = 1;
         st.S.a = a[i];
-        st.S.has_ax = i == 0;
+        st.S.has_ax = k == 0;
         st.S.a_x = a_x;
         st.S.ay_mode = (last && a_y != 0.0) ? 1 : 0;
         st.S.a_y = a_y;
         int s, t;
-        pingpong(d, i, s, t);
+        pingpong(d, k, s, t);
         st.src = B_X;
         st.dst = t;
-        st.src2 = i == 0 ? -1 : s;
+        st.src2 = k == 0 ? -1 : s;
         st.S.narr = narr;
         st.S.x_arr = st.S.y_arr = tot;
         need(P, B_X, tot * narr);
@@ -495,6 +531,22 @@ int kinetic_dotin_sweep(int d, int idim, const int *n, int bc, const int *nx, co
 
 int report(int code, const char *msg) { return fail(code, "%s", msg); }
 int report_cuda(cudaError_t e, const char *what) { return cuda_fail(e, what); }
+
+int plan_magicfilter(int d, const int *n, const int *bc, const int *order, Plan &P) {
+    return order ? plan_md_n(OP_MD, d, n, bc, order, P)
+                 : plan_md_t(OP_MD, d, n, bc, nullptr, nullptr, 1, P);
+}
+int plan_kinetic(int d, const int *n, const int *bc, const double *a, double a_x,
+                 const int *order, Plan &P) {
+    return plan_kin(d, n, bc, a, a_x, 0.0, P, 1, order);
+}
+const double *filter_table() { return h_ftab; }
+int current_mode() { return t_mode; }
+int *device_status(int &rc) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    DevState *s = dev_state(rc);
+    return s ? (int *)s->status.p : nullptr;
+}
 }  // namespace lcg
 
 // =============================== exported C ABI ===============================

@@ -48,19 +48,19 @@ __device__ __forceinline__ double fetch(const Sweep &S, const double *__restrict
     return x[l + (long long)S.nL * (off + in_pext * r)];
 }
 
-template <int KIND, int NT>
-__global__ void __launch_bounds__(kThreads) sweep_fp64_kernel(const Sweep S) {
+// One block of the sweep: lines [bx*32, bx*32+32) x output chunk by of array
+// bz.  `tile` and `red` are the block's shared staging buffers.
+template <int KIND, int NT, int QC>
+__device__ __forceinline__ void sweep_block(const Sweep &S, long long bx, int by, int bz,
+                                            double *tile, double *red, long long dot_index) {
     constexpr int NCH = KIND == KCONV ? 1 : 2;
-    constexpr int QC = Chunk<KIND>::QC;
     constexpr int SPAN = QC + NT - 1;
     constexpr int NROW = SPAN * NCH;
-    __shared__ double tile[NROW * kPad];
-    __shared__ double red[kWarps];
 
-    const int arr = blockIdx.z;
+    const int arr = bz;
     const long long nlines = (long long)S.nL * S.nR;
-    const long long g0 = (long long)blockIdx.x * kLines;
-    const int qc0 = S.qlo + blockIdx.y * QC;
+    const long long g0 = bx * kLines;
+    const int qc0 = S.qlo + by * QC;
     const int upfil = S.lowfil + NT - 1;
     const int plast = S.qhi + upfil;  // last logical input index any output needs
     const long long in_pext = (long long)S.in_ext * NCH;
@@ -162,9 +162,53 @@ __global__ void __launch_bounds__(kThreads) sweep_fp64_kernel(const Sweep S) {
         if (threadIdx.x == 0) {
             double s = 0.0;
             for (int i = 0; i < kWarps; ++i) s += red[i];
-            const long long b = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-            S.dot_part[b] = s;
+            S.dot_part[dot_index] = s;
         }
+    }
+}
+
+template <int KIND, int NT, int QC>
+__global__ void __launch_bounds__(kThreads) sweep_fp64_kernel(const __grid_constant__ Sweep S) {
+    constexpr int NROW = (QC + NT - 1) * (KIND == KCONV ? 1 : 2);
+    __shared__ double tile[NROW * kPad];
+    __shared__ double red[kWarps];
+    const long long b = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    sweep_block<KIND, NT, QC>(S, blockIdx.x, blockIdx.y, blockIdx.z, tile, red, b);
+}
+
+// Blocks of one sweep (all narr arrays).
+__host__ __device__ __forceinline__ long long blocks_of(const Sweep &S, int qc) {
+    const long long nlines = (long long)S.nL * S.nR;
+    const long long nq = S.qhi - S.qlo + 1;
+    return ((nlines + kLines - 1) / kLines) * ((nq + qc - 1) / qc) * S.narr;
+}
+
+// Persistent form over a list of sweeps of the same kind and filter (one
+// per grid of a batch of uneven grids): the blocks of all sweeps are numbered
+// consecutively (prefix[i] = first block of sweep i) and each CTA walks them
+// with a grid stride, locating a block's sweep by binary search.
+template <int KIND, int NT, int QC>
+__global__ void __launch_bounds__(kThreads)
+sweep_fp64_batch_kernel(const Sweep *__restrict__ descs, const long long *__restrict__ prefix,
+                        int nsweeps) {
+    constexpr int NROW = (QC + NT - 1) * (KIND == KCONV ? 1 : 2);
+    __shared__ double tile[NROW * kPad];
+    __shared__ double red[kWarps];
+    const long long total = prefix[nsweeps];
+    for (long long b = blockIdx.x; b < total; b += gridDim.x) {
+        int lo = 0, hi = nsweeps - 1;                    // last i with prefix[i] <= b
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (prefix[mid] <= b) lo = mid;
+            else hi = mid - 1;
+        }
+        const Sweep &S = descs[lo];
+        const long long lb = b - prefix[lo];
+        const long long gx = ((long long)S.nL * S.nR + kLines - 1) / kLines;
+        const int gy = (S.qhi - S.qlo + QC) / QC;
+        sweep_block<KIND, NT, QC>(S, lb % gx, (int)((lb / gx) % gy), (int)(lb / (gx * gy)), tile,
+                                  red, 0);
+        __syncthreads();                                 // tile reused by the next block
     }
 }
 
@@ -182,14 +226,54 @@ __global__ void dot_reduce_kernel(const double *__restrict__ part, long long cou
     if (threadIdx.x == 0) *out = accumulate ? *out + red[0] : red[0];
 }
 
-template <int KIND, int NT>
+template <int KIND, int NT, int QC = Chunk<KIND>::QC>
 cudaError_t launch_t(const Sweep &S, cudaStream_t st) {
     const long long nlines = (long long)S.nL * S.nR;
     const int nq = S.qhi - S.qlo + 1;
-    dim3 grid((unsigned)((nlines + kLines - 1) / kLines),
-              (unsigned)((nq + Chunk<KIND>::QC - 1) / Chunk<KIND>::QC), (unsigned)S.narr);
-    sweep_fp64_kernel<KIND, NT><<<grid, kThreads, 0, st>>>(S);
+    dim3 grid((unsigned)((nlines + kLines - 1) / kLines), (unsigned)((nq + QC - 1) / QC),
+              (unsigned)S.narr);
+    sweep_fp64_kernel<KIND, NT, QC><<<grid, kThreads, 0, st>>>(S);
     return cudaGetLastError();
+}
+
+template <int KIND, int NT, int QC>
+cudaError_t launch_batch_t(const Sweep *descs, const long long *prefix, int nsweeps, int grid,
+                           cudaStream_t st) {
+    sweep_fp64_batch_kernel<KIND, NT, QC><<<grid, kThreads, 0, st>>>(descs, prefix, nsweeps);
+    return cudaGetLastError();
+}
+
+template <int KIND, int NT, int QC>
+int batch_grid_t() {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_fp64_batch_kernel<KIND, NT, QC>,
+                                                  kThreads, 0);
+    return (sms > 0 ? sms : 148) * (per > 0 ? per : 1);
+}
+
+template <int QC>
+int batch_grid_qc(int kind, int ntaps) {
+    if (kind == KCONV && ntaps == 16) return batch_grid_t<KCONV, 16, QC>();
+    if (kind == KCONV && ntaps == 29) return batch_grid_t<KCONV, 29, QC>();
+    if (kind == KDEC && ntaps == 8) return batch_grid_t<KDEC, 8, QC / 2>();
+    if (kind == KDEC && ntaps == 16) return batch_grid_t<KDEC, 16, QC / 2>();
+    if (kind == KREC && ntaps == 8) return batch_grid_t<KREC, 8, QC / 2>();
+    if (kind == KREC && ntaps == 16) return batch_grid_t<KREC, 16, QC / 2>();
+    return 0;
+}
+
+template <int QC>
+cudaError_t launch_batch_qc(int kind, int ntaps, const Sweep *descs, const long long *prefix,
+                            int nsweeps, int grid, cudaStream_t st) {
+    if (kind == KCONV && ntaps == 16) return launch_batch_t<KCONV, 16, QC>(descs, prefix, nsweeps, grid, st);
+    if (kind == KCONV && ntaps == 29) return launch_batch_t<KCONV, 29, QC>(descs, prefix, nsweeps, grid, st);
+    if (kind == KDEC && ntaps == 8) return launch_batch_t<KDEC, 8, QC / 2>(descs, prefix, nsweeps, grid, st);
+    if (kind == KDEC && ntaps == 16) return launch_batch_t<KDEC, 16, QC / 2>(descs, prefix, nsweeps, grid, st);
+    if (kind == KREC && ntaps == 8) return launch_batch_t<KREC, 8, QC / 2>(descs, prefix, nsweeps, grid, st);
+    if (kind == KREC && ntaps == 16) return launch_batch_t<KREC, 16, QC / 2>(descs, prefix, nsweeps, grid, st);
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace
@@ -208,6 +292,22 @@ cudaError_t launch_sweep_fp64(const Sweep &S, cudaStream_t st) {
     if (S.kind == KDEC && S.ntaps == 16) return launch_t<KDEC, 16>(S, st);
     if (S.kind == KREC && S.ntaps == 8) return launch_t<KREC, 8>(S, st);
     if (S.kind == KREC && S.ntaps == 16) return launch_t<KREC, 16>(S, st);
+    return cudaErrorInvalidValue;
+}
+
+long long sweep_fp64_batch_blocks(const Sweep &S, int qc) {
+    return blocks_of(S, S.kind == KCONV ? qc : qc / 2);
+}
+
+int sweep_fp64_batch_grid(int kind, int ntaps, int qc) {
+    return qc == 64 ? batch_grid_qc<64>(kind, ntaps) : batch_grid_qc<32>(kind, ntaps);
+}
+
+cudaError_t launch_sweep_fp64_batch(int kind, int ntaps, int qc, const Sweep *descs,
+                                    const long long *prefix, int nsweeps, int grid,
+                                    cudaStream_t st) {
+    if (qc == 64) return launch_batch_qc<64>(kind, ntaps, descs, prefix, nsweeps, grid, st);
+    if (qc == 32) return launch_batch_qc<32>(kind, ntaps, descs, prefix, nsweeps, grid, st);
     return cudaErrorInvalidValue;
 }
 

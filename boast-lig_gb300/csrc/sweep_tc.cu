@@ -108,6 +108,23 @@ void tc_filter_split(const double *taps, int ntaps, double a, int sch, TcFilter 
     }
 }
 
+long long sweep_tc_tiles(const Sweep &S) {
+    return tck::tile_count_for(S, S.kind == KCONV ? 64 : 32);
+}
+
+bool sweep_tc_batch_supported(int kind, int ntaps) {
+    return kind == KCONV && (ntaps == 16 || ntaps == 29);
+}
+
+cudaError_t launch_sweep_tc_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
+                                  int nsweeps, const TcFilter &F, int sch, int *status,
+                                  cudaStream_t st) {
+    if (sch == SCH_EXACT) return tck::launch_exact_batch(kind, ntaps, descs, prefix, nsweeps, F, status, st);
+    if (sch == SCH_BF16X3) return tck::launch_bf16x3_batch(kind, ntaps, descs, prefix, nsweeps, F, status, st);
+    if (sch == SCH_TF32X3) return tck::launch_tf32x3_batch(kind, ntaps, descs, prefix, nsweeps, F, status, st);
+    return cudaErrorInvalidValue;
+}
+
 cudaError_t launch_sweep_tc(const Sweep &S, const TcFilter &F, int sch, int *status,
                             cudaStream_t st) {
     if (sch == SCH_EXACT) return tck::launch_exact(S, F, status, st);

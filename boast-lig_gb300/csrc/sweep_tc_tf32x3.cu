@@ -1,5 +1,6 @@
 // Tensor-core sweep, scheme SCH_TF32X3: convolution (16, 29 taps) and
-// wavelet decompose / recompose (8, 16 polyphase taps) instantiations.
+// wavelet decompose / recompose (8, 16 polyphase taps) instantiations, and
+// the batched convolution forms.
 #include "tc_kernel.cuh"
 
 namespace lcg {
@@ -12,6 +13,15 @@ cudaError_t launch_tf32x3(const Sweep &S, const TcFilter &F, int *status, cudaSt
     if (S.kind == KDEC && S.ntaps == 16) return launch<KDEC, 16, SCH_TF32X3>(S, F, status, st);
     if (S.kind == KREC && S.ntaps == 8) return launch<KREC, 8, SCH_TF32X3>(S, F, status, st);
     if (S.kind == KREC && S.ntaps == 16) return launch<KREC, 16, SCH_TF32X3>(S, F, status, st);
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_tf32x3_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
+                               int nsweeps, const TcFilter &F, int *status, cudaStream_t st) {
+    if (kind == KCONV && ntaps == 16)
+        return launch_batch<KCONV, 16, SCH_TF32X3>(descs, prefix, nsweeps, F, status, st);
+    if (kind == KCONV && ntaps == 29)
+        return launch_batch<KCONV, 29, SCH_TF32X3>(descs, prefix, nsweeps, F, status, st);
     return cudaErrorInvalidValue;
 }
 

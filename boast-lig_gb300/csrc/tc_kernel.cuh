@@ -324,9 +324,32 @@ __device__ __forceinline__ int filter_index(int c, int c2) {
     return c == 0 ? (c2 == 0 ? 1 : 3) : (c2 == 0 ? 0 : 2);          // KREC
 }
 
-template <int KIND, int NT, int SCH>
+// Where tile `tile` of a launch lives: its sweep and its index within the
+// sweep.  A batched launch (BATCH) covers a list of sweeps of the same kind
+// and filter, one per grid of a batch of uneven grids, whose tiles are
+// numbered consecutively (prefix[i] = first tile of sweep i).
+struct TileLoc {
+    const Sweep *S;
+    long long t;
+};
+
+template <bool BATCH>
+__device__ __forceinline__ TileLoc locate(const Sweep &S0, const Sweep *descs,
+                                          const long long *prefix, int nsweeps, long long tile) {
+    if (!BATCH) return {&S0, tile};
+    int lo = 0, hi = nsweeps - 1;                        // last i with prefix[i] <= tile
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return {descs + lo, tile - prefix[lo]};
+}
+
+template <int KIND, int NT, int SCH, bool BATCH>
 __global__ void __launch_bounds__(kThreads, 1)
-sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
+sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilter F, int *status,
+                const Sweep *__restrict__ descs, const long long *__restrict__ prefix, int nsweeps) {
     using G = Geom<KIND, NT, SCH>;
     constexpr int NCH = G::NCH;
     extern __shared__ uint8_t smem_raw[];
@@ -345,13 +368,9 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
     const uint32_t bX_full[2] = {saddr(&bars[6]), saddr(&bars[7])};
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const long long nlines = (long long)S.nL * S.nR;
-    const long long nlb = (nlines + kM - 1) / kM;
-    const int nq = S.qhi - S.qlo + 1;                 // output positions
-    const int nch = (nq + G::QP - 1) / G::QP;
-    const long long ntiles = nlb * nch * S.narr;
-    const int upfil = S.lowfil + NT - 1;
-    const int plast = S.qhi + upfil;                  // last input position any output needs
+    const long long ntiles = BATCH ? prefix[nsweeps]
+                                   : ((long long)S0.nL * S0.nR + kM - 1) / kM *
+                                         ((S0.qhi - S0.qlo + G::QP) / G::QP) * S0.narr;
     const int kneed = NCH * (G::QP + NT - 1);         // input elements the tile's outputs use
 
     if (warp == 0) {
@@ -399,14 +418,20 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
         constexpr int H = G::KT / 2;                                  // multiple of 8
         const int half = lane >> 4;
         const int row = warp * 16 + (lane & 15);
-        const long long *xbits = reinterpret_cast<const long long *>(S.x);
-        const long long in_ext = S.in_ext;
         uint32_t it = 0;
         for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
             if (it > 0 && !bar_wait(bA_empty, (it - 1) & 1)) { alive = false; break; }
-            const int ch = (int)(tile % nch);
-            const long long lb = (tile / nch) % nlb;
-            const int arr = (int)(tile / (nch * nlb));
+            const TileLoc loc = locate<BATCH>(S0, descs, prefix, nsweeps, tile);
+            const Sweep &S = *loc.S;
+            const long long nlines = (long long)S.nL * S.nR;
+            const long long nlb = (nlines + kM - 1) / kM;
+            const int nch = (S.qhi - S.qlo + G::QP) / G::QP;
+            const int ch = (int)(loc.t % nch);
+            const long long lb = (loc.t / nch) % nlb;
+            const int arr = (int)(loc.t / (nch * nlb));
+            const int plast = S.qhi + S.lowfil + NT - 1;                // last input position used
+            const long long *xbits = reinterpret_cast<const long long *>(S.x);
+            const long long in_ext = S.in_ext;
             const int p0 = S.qlo + ch * G::QP + S.lowfil;               // first input position
             const int pstart = S.bc == BC_PERIODIC ? imod(p0, S.n) : 0;
             const bool onewrap = S.n >= G::KT;
@@ -564,7 +589,6 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
         const int ew = warp - kProducers / 32;
         const int lq = ew & 3, hf = ew >> 2;
         const int row = lq * 32 + lane;
-        const long long out_pext = (long long)S.out_ext * NCH;
         double dot = 0.0;
         uint32_t it = 0;
         for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
@@ -572,10 +596,16 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
             const int Er = rowE_epi[(it & 1) * kM + row];
             if (!bar_wait(bT_full[hf], it & 1)) { alive = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const int ch = (int)(tile % nch);
-            const long long lb = (tile / nch) % nlb;
-            const int arr = (int)(tile / (nch * nlb));
+            const TileLoc loc = locate<BATCH>(S0, descs, prefix, nsweeps, tile);
+            const Sweep &S = *loc.S;
+            const long long nlines = (long long)S.nL * S.nR;
+            const long long nlb = (nlines + kM - 1) / kM;
+            const int nch = (S.qhi - S.qlo + G::QP) / G::QP;
+            const int ch = (int)(loc.t % nch);
+            const long long lb = (loc.t / nch) % nlb;
+            const int arr = (int)(loc.t / (nch * nlb));
             const int qc0 = S.qlo + ch * G::QP;
+            const long long out_pext = (long long)S.out_ext * NCH;
             const long long g = lb * kM + row;
             const bool valid = g < nlines;
             const long long l = valid ? g % S.nL : 0, rr = valid ? g / S.nL : 0;
@@ -652,7 +682,7 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
                 }
             }
         }
-        if (S.has_dot) {
+        if (S0.has_dot) {
             for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
             if (lane == 0) red[ew] = dot;
         }
@@ -665,28 +695,51 @@ sweep_tc_kernel(const Sweep S, const TcFilter F, int *status) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
                      "r"(G::TMEM_COLS)
                      : "memory");
-    if (S.has_dot && tid == 0) {
+    if (S0.has_dot && tid == 0) {
         double sdot = 0.0;
         for (int i = 0; i < 8; ++i) sdot += red[i];
-        S.dot_part[blockIdx.x] = sdot;
+        S0.dot_part[blockIdx.x] = sdot;
     }
 }
 
-template <int KIND, int NT, int SCH>
-cudaError_t launch(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st) {
+template <int KIND, int NT, int SCH, bool BATCH>
+cudaError_t set_smem_attr() {
     using G = Geom<KIND, NT, SCH>;
     static bool attr[64] = {};   // the attribute is set once per device
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64 || !attr[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(sweep_tc_kernel<KIND, NT, SCH>,
+        cudaError_t e = cudaFuncSetAttribute(sweep_tc_kernel<KIND, NT, SCH, BATCH>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM);
         if (e != cudaSuccess) return e;
         if (dev >= 0 && dev < 64) attr[dev] = true;
     }
+    return cudaSuccess;
+}
+
+template <int KIND, int NT, int SCH>
+cudaError_t launch(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st) {
+    using G = Geom<KIND, NT, SCH>;
+    cudaError_t e = set_smem_attr<KIND, NT, SCH, false>();
+    if (e != cudaSuccess) return e;
     const long long tiles = tile_count_for(S, G::QP);
     const int grid = (int)(tiles < sm_count() ? tiles : sm_count());
-    sweep_tc_kernel<KIND, NT, SCH><<<grid, kThreads, G::SMEM, st>>>(S, F, status);
+    sweep_tc_kernel<KIND, NT, SCH, false><<<grid, kThreads, G::SMEM, st>>>(S, F, status, nullptr,
+                                                                           nullptr, 0);
+    return cudaGetLastError();
+}
+
+// Batched launch over nsweeps descriptors (device arrays); S0 only carries
+// has_dot = 0.  One CTA per SM.
+template <int KIND, int NT, int SCH>
+cudaError_t launch_batch(const Sweep *descs, const long long *prefix, int nsweeps,
+                         const TcFilter &F, int *status, cudaStream_t st) {
+    using G = Geom<KIND, NT, SCH>;
+    cudaError_t e = set_smem_attr<KIND, NT, SCH, true>();
+    if (e != cudaSuccess) return e;
+    Sweep S0{};
+    sweep_tc_kernel<KIND, NT, SCH, true><<<sm_count(), kThreads, G::SMEM, st>>>(S0, F, status, descs,
+                                                                                prefix, nsweeps);
     return cudaGetLastError();
 }
 

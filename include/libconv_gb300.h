@@ -230,6 +230,52 @@ int d_sfrf_cost(int d, const int *n, const int *bc, int narr, long long *cost);
 int d_kin_cost(int d, const int *n, const int *bc, long long *cost);
 int d_dwt_sym8_cost(int d, const int *n, const int *bc, long long *cost);
 
+/* ---------------------------------------------------------------------
+ * Batched 3D operators over many grids of different sizes (extension: no
+ * counterpart in the generated code, which runs one grid per call), for the
+ * orbitals of uneven localisation regions.  Grid g has dims[3g..3g+2]; the
+ * grids are packed back to back (each in Fortran order) in x, y_mf and
+ * y_kin, at the element offsets libconv_batch_offsets reports.
+ *   - MagicFilter3D (mf_bc != NULL): sfrf_ld_narr of each grid, output sizes
+ *     by mf_bc (grow: n + 15 per axis);
+ *   - Kinetic3D (kin_bc != NULL; periodic or free): d_kin of each grid with
+ *     kin_a[3], kin_ax (a_y = 0).
+ * Each sweep stage of an operator is ONE persistent launch over the sweeps of
+ * all grids; a run is a CUDA graph of those launches (captured on the first
+ * run on a stream; the legacy default stream runs the launches uncaptured).
+ * The batch keeps the compute mode of the thread that created it and owns
+ * its device workspaces (allocated at creation).  libconv_batch_tune times
+ * every engine and sweep order the mode allows on the caller's buffers and
+ * keeps the fastest, recorded in the JSON file $LIBCONV_GB300_TUNE_CACHE
+ * (default $HOME/.cache/libconv_gb300_tune.json) and reused by later
+ * batches of the same shapes on the same GPU model and mode.
+ * --------------------------------------------------------------------- */
+typedef struct libconv_batch libconv_batch;
+#define LIBCONV_BATCH_OP_MF   0
+#define LIBCONV_BATCH_OP_KIN  1
+/* engines: FP64 sweep with 64- or 32-output chunks, or the tensor-core sweep
+ * of the batch's mode (not in LIBCONV_MODE_FP64) */
+#define LIBCONV_ENGINE_FP64_Q64  0
+#define LIBCONV_ENGINE_FP64_Q32  1
+#define LIBCONV_ENGINE_TC        2
+int libconv_batch_create(libconv_batch **b, int ngrids, const int *dims, const int *mf_bc,
+                         const int *kin_bc, const double *kin_a, double kin_ax);
+int libconv_batch_sizes(const libconv_batch *b, long long *in_elems, long long *mf_elems,
+                        long long *kin_elems);
+/* ngrids + 1 offsets each (last = total); NULL arrays are skipped */
+int libconv_batch_offsets(const libconv_batch *b, long long *in_off, long long *mf_off,
+                          long long *kin_off);
+/* order: the three axes in sweep order; for the MagicFilter order[0] = -1
+ * selects the reference's rotating sweeps (transpose = 1) */
+int libconv_batch_set_config(libconv_batch *b, int op, int engine, const int *order);
+int libconv_batch_get_config(const libconv_batch *b, int op, int *engine, int *order, int *tuned);
+int libconv_batch_tune(libconv_batch *b, const double *x, double *y_mf, double *y_kin,
+                       void *stream);
+/* device pointers; enqueues only (check with libconv_gb300_check) */
+int libconv_batch_run(libconv_batch *b, const double *x, double *y_mf, double *y_kin,
+                      void *stream);
+int libconv_batch_destroy(libconv_batch *b);
+
 #ifdef __cplusplus
 }
 #endif
