@@ -15,8 +15,14 @@ uniform [-1, 1], details uniform [-1, 1] x 1e-3) into 96^3, then analysis
 back; metric: 96^3 grid points per second through both transforms.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload mfkin128|wavelet96]
+                  [--workload mfkin128|wavelet96|orbitals512]
                   [--mode tc_exact|fp64|tc_bf16x3|tc_tf32x3]
+
+Workload orbitals512: 512 orbitals with axes uniform in {24..72} (seed 7),
+Gaussian envelope times unit-RMS noise; MagicFilter3D free grow and
+Kinetic3D free per orbital, batched (one persistent launch per sweep stage,
+CUDA graph, autotuned); the line also times the same work as per-orbital
+calls of the single-grid entry points.
 
 Modes: tc_exact (default) runs the tensor-core exact-digit sweeps (FP64
 accuracy); fp64 the FP64 FMA sweeps; tc_bf16x3 / tc_tf32x3 the split-precision
@@ -178,7 +184,33 @@ class Wavelet96:
     pairs_exact = 28
 
 
-WORKLOADS = {'mfkin128': MfKin128(), 'wavelet96': Wavelet96()}
+class Orbitals512:
+    """512 orbitals of uneven sizes: MagicFilter3D free grow + Kinetic3D free."""
+    name = 'orbitals512'
+    metric = ('grid pts/s, 512 uneven orbitals (axes U{24..72}): MagicFilter3D free grow + '
+              'Kinetic3D free, batched')
+    count = 512
+    a = [-0.5 / HGRID ** 2] * 3
+
+    def dims(self):
+        package()
+        from boast_lig_gb300 import inputs
+        return [[int(v) for v in d] for d in inputs.orbital_dims(7, self.count)]
+
+    def base(self, count=None):
+        package()
+        from boast_lig_gb300 import inputs
+        return [inputs.orbital(1000 + g, d, h=HGRID).ravel(order='F')
+                for g, d in enumerate(self.dims())]
+
+    def cpu_work(self, O, x, bufs, d):
+        ny = [v + 15 for v in d]
+        y, tx, w1, w2 = bufs
+        O.call('oracle_d_sfrf_ld_narr', 3, d, [1, 1, 1], d, ny, 1, x, y, w1, w2)
+        O.call('oracle_d_kin', 3, d, [2, 2, 2], x, tx, w1, w2, np.array(self.a), 0.0, 0.0)
+
+
+WORKLOADS = {'mfkin128': MfKin128(), 'wavelet96': Wavelet96(), 'orbitals512': Orbitals512()}
 
 
 class Clocks:
@@ -248,6 +280,32 @@ def cpu_run(W, grids, threads, steps, warmup):
     return times, threads * W.n_in
 
 
+def cpu_run_orbitals(W, xs, dims, threads, seconds):
+    """Oracle MF free grow + kinetic free over orbitals taken round robin by
+    host threads until about `seconds` have passed; returns (points, time)."""
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    O.lib()
+    big = max(int(np.prod([v + 15 for v in d])) for d in dims)
+    bufs = [[np.zeros(big) for _ in range(4)] for _ in range(threads)]
+    done = [0] * threads
+    t0 = time.perf_counter()
+
+    def work(t):
+        g = t
+        while time.perf_counter() - t0 < seconds and g < len(xs):
+            W.cpu_work(O, xs[g], bufs[t], dims[g])
+            done[t] += xs[g].size
+            g += threads
+
+    th = [threading.Thread(target=work, args=(t,)) for t in range(threads)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    return sum(done), time.perf_counter() - t0
+
+
 def cpu_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -267,11 +325,34 @@ def cpu_baseline_sample(W, grids):
                       f'{W.name} operators, C oracle, median step {t:.3f} s'}
 
 
+def run_reference_orbitals(args, W):
+    dims = W.dims()
+    xs = W.base()
+    th = cpu_threads()
+    vals = []
+    for _ in range(max(args.steps, 1)):
+        pts, t = cpu_run_orbitals(W, xs, dims, th, 10.0)
+        vals.append(pts / t)
+    v = float(np.median(vals))
+    line = {'impl': 'reference', 'metric': W.metric, 'value': v, 'unit': UNIT,
+            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': sum(x.size for x in xs) / v * 1e3, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded)',
+            'config': {'workload': f'512 orbitals, oracle MF free grow + kinetic free, {th} host '
+                                   'threads taking orbitals round robin, ~10 s sample per step'},
+            'cpu_baseline': {'value': v, 'unit': UNIT, 'cores': th, 'kind': 'port',
+                             'sample': 'orbitals processed in ~10 s per step, C oracle'},
+            'e2e': {'value': v, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get('RANK', '0'))
     if rank != 0:
         return
     W = WORKLOADS[args.workload]
+    if W.name == 'orbitals512':
+        return run_reference_orbitals(args, W)
     grids = W.base(4)
     th = cpu_threads()
     times, pts = cpu_run(W, grids, th, args.steps, max(args.warmup, 1))
@@ -295,10 +376,177 @@ MODES = {'fp64': 'MODE_FP64', 'tc_exact': 'MODE_TC_EXACT', 'tc_bf16x3': 'MODE_TC
          'tc_tf32x3': 'MODE_TC_TF32X3'}
 
 
+def run_orbitals(args, W):
+    """Batched uneven orbitals: one graph launch per step (6 persistent sweep
+    launches over all orbitals, tuned engine and sweep order), against the
+    same operators called grid by grid through the single-grid entry points."""
+    import torch
+    pkg = package()
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl', device_id=dev)
+    dims_all = W.dims()
+    xs_all = W.base()
+    # orbitals are partitioned across ranks, balanced by size (largest first)
+    order = sorted(range(len(dims_all)), key=lambda g: -int(np.prod(dims_all[g])))
+    mine = [g for i, g in enumerate(order) if i % world == rank]
+    dims = [dims_all[g] for g in mine]
+    xs = [xs_all[g] for g in mine]
+    pkg.set_mode(getattr(pkg, MODES[args.mode]))
+    B = pkg.Batch(dims, mf_bc=[1, 1, 1], kin_bc=[2, 2, 2], kin_a=W.a)
+    n_in, n_mf, n_kin = B.sizes()
+    host_x = torch.from_numpy(np.concatenate(xs)).pin_memory()
+    x = host_x.to(dev)
+    y_mf = torch.empty(n_mf, dtype=torch.float64, device=dev)
+    y_kin = torch.empty(n_kin, dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    t0 = time.perf_counter()
+    if not args.no_tune:
+        B.tune(x, y_mf, y_kin, stream=stream)
+    tune_s = time.perf_counter() - t0
+    for _ in range(max(args.warmup, 3)):
+        B.run(x, y_mf, y_kin, stream=stream)
+    pkg.check(stream)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    clocks = Clocks(local)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    start.record(stream)
+    for _ in range(args.steps):
+        B.run(x, y_mf, y_kin, stream=stream)
+    stop.record(stream)
+    stop.synchronize()
+    barrier()
+    ck = clocks.stop()
+    pkg.check(stream)
+    ms = start.elapsed_time(stop)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = t.item()
+        tot = torch.tensor([float(n_in)], device=dev)
+        dist.all_reduce(tot)
+        pts_step = tot.item()
+    else:
+        pts_step = n_in
+    value = pts_step * args.steps / (ms / 1e3)
+
+    # the same work grid by grid through the single-grid device entry points
+    in_off, mf_off, kin_off = B.offsets()
+    w1 = torch.empty(max(int(np.prod([v + 15 for v in d])) for d in dims), dtype=torch.float64,
+                     device=dev)
+    w2 = torch.empty_like(w1)
+    mf_k, kin_k = pkg.Kernel('d_sfrf_ld_narr'), pkg.Kernel('d_kin')
+    sp = stream.cuda_stream
+    xp, mp, kp = x.data_ptr(), y_mf.data_ptr(), y_kin.data_ptr()
+
+    def per_grid():
+        for g, d in enumerate(dims):
+            ny = [v + 15 for v in d]
+            mf_k.run_dev(3, d, [1, 1, 1], d, ny, 1, xp + 8 * in_off[g], mp + 8 * mf_off[g], w1, w2,
+                         stream=sp)
+            kin_k.run_dev(3, d, [2, 2, 2], xp + 8 * in_off[g], kp + 8 * kin_off[g], w1, w2, W.a,
+                          0.0, 0.0, stream=sp)
+
+    per_grid()
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(2):
+        per_grid()
+    e1.record(stream)
+    e1.synchronize()
+    per_grid_ms = e0.elapsed_time(e1) / 2
+
+    # e2e: pinned host orbitals in, both outputs back, every step
+    host_mf = torch.empty(n_mf, dtype=torch.float64).pin_memory()
+    host_kin = torch.empty(n_kin, dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            x.copy_(host_x, non_blocking=True)
+            B.run(x, y_mf, y_kin, stream=stream)
+            host_mf.copy_(y_mf, non_blocking=True)
+            host_kin.copy_(y_kin, non_blocking=True)
+        stream.synchronize()
+
+    e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(max(2, min(args.steps, 5))):
+        e2e_step()
+    barrier()
+    e_t = (time.perf_counter() - t0) / max(2, min(args.steps, 5))
+    e2e = {'value': pts_step / e_t, 'unit': UNIT, 'h2d_bytes_per_step': 8 * n_in,
+           'd2h_bytes_per_step': 8 * (n_mf + n_kin),
+           'note': 'libconv_batch_run (graph) on the packed orbitals, H2D of x and D2H of '
+                   'both outputs from pinned host memory inside the timed region'}
+
+    # roofline of the step (6 batched sweeps): MF grow moves 8 (in + out) per
+    # sweep over the growing sizes, the kinetic 16 + 24 + 24 B per point
+    mf_bytes = 0
+    for d in dims:
+        a, b_, c = d
+        A, Bq, C = a + 15, b_ + 15, c + 15
+        mf_bytes += 8 * ((a * b_ * c + A * b_ * c) + (A * b_ * c + A * Bq * c) + (A * Bq * c + A * Bq * C))
+    kin_bytes = 64 * n_in
+    pk = peaks()
+    achieved = (mf_bytes + kin_bytes) / (ms / args.steps / 1e3) / 1e9
+    eng = {0: 'fp64 q64', 1: 'fp64 q32', 2: 'tensor core'}
+    cfg = {'magicfilter3d': B.get_config(pkg.BATCH_OP_MF), 'kinetic3d': B.get_config(pkg.BATCH_OP_KIN)}
+    line = {'metric': W.metric, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+            'warmup': max(args.warmup, 3), 'ms_per_step': ms / args.steps, 'higher_is_better': True,
+            'scaling': 'weak' if world == 1 else 'strong', 'vs_baseline': None,
+            'dtype': 'f64' if args.mode in ('fp64', 'tc_exact') else args.mode,
+            'data': 'synthetic (seeded orbitals: Gaussian envelope x unit-RMS noise, h=0.45)',
+            'config': {'workload': f'{len(dims)} orbitals per GPU (axes U{{24..72}}, seed 7, '
+                                   f'{n_in / 1e6:.1f} M points), MagicFilter3D free grow + '
+                                   'Kinetic3D free, one libconv_batch_run (CUDA graph of 6 '
+                                   'persistent sweeps) per step', 'mode': args.mode,
+                       'tuned': {k: {'engine': eng[v[0]], 'order': v[1]} for k, v in cfg.items()},
+                       'tune_seconds': tune_s,
+                       'per_grid_calls_ms_per_step': per_grid_ms,
+                       'batched_speedup_vs_per_grid_calls': per_grid_ms / (ms / args.steps),
+                       'l2': f'inputs larger than L2 ({8 * n_in / 1e6:.0f} MB in, '
+                             f'{8 * n_mf / 1e6:.0f} MB MF out)'},
+            'clocks': ck, 'e2e': e2e, 'gpu_launches': args.steps * 6,
+            'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': pk['hbm'], 'unit': 'GB/s',
+                         'frac': achieved / pk['hbm'], 'traffic': None,
+                         'kernel': 'whole step: 6 batched sweeps (3 MF grow, 3 kinetic)',
+                         'peak_source': pk['source']}}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        th = cpu_threads()
+        pts, t = cpu_run_orbitals(W, xs, dims, th, 10.0)
+        line['cpu_baseline'] = {'value': pts / t, 'unit': UNIT, 'cores': th, 'kind': 'port',
+                                'sample': f'{pts / 1e6:.1f} M orbital points in {t:.1f} s, '
+                                          'C oracle, orbitals round robin over host threads'}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    B.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
 def run_gpu(args):
     import torch
     pkg = package()
     W = WORKLOADS[args.workload]
+    if W.name == 'orbitals512':
+        return run_orbitals(args, W)
     world = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
     local = int(os.environ.get('LOCAL_RANK', '0'))
@@ -459,6 +707,8 @@ def main():
     ap.add_argument('--workload', default='mfkin128', choices=list(WORKLOADS))
     ap.add_argument('--grids', type=int, default=32)
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline sample')
+    ap.add_argument('--no-tune', action='store_true',
+                    help='orbitals512: use the cached or default batch configuration')
     ap.add_argument('--mode', default='tc_exact', choices=list(MODES),
                     help='tc_exact: tensor-core exact-digit sweeps (FP64-accurate); fp64: FP64 '
                          'FMA; tc_bf16x3 / tc_tf32x3: split precision (error reported)')
