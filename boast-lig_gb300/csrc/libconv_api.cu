@@ -564,6 +564,7 @@ const char *libconv_gb300_strerror(int s) {
     case LIBCONV_ENOMEM: return "device allocation failed";
     case LIBCONV_EMODE: return "unknown compute mode";
     case LIBCONV_ETIMEOUT: return "device-side wait timed out";
+    case LIBCONV_ENUMERIC: return "non-finite result";
     default: return "unknown status";
     }
 }

@@ -39,6 +39,7 @@ extern "C" {
 #define LIBCONV_ENOMEM   -5   /* device allocation failed */
 #define LIBCONV_EMODE    -6   /* unknown compute mode */
 #define LIBCONV_ETIMEOUT -7   /* a bounded device-side wait gave up (status word set) */
+#define LIBCONV_ENUMERIC -8   /* a solve produced a non-finite residual */
 
 #define LIBCONV_BC_SHRINK   -1
 #define LIBCONV_BC_PERIODIC  0
@@ -275,6 +276,56 @@ int libconv_batch_tune(libconv_batch *b, const double *x, double *y_mf, double *
 int libconv_batch_run(libconv_batch *b, const double *x, double *y_mf, double *y_kin,
                       void *stream);
 int libconv_batch_destroy(libconv_batch *b);
+
+/* ---------------------------------------------------------------------
+ * Shifted kinetic solves (extension: no counterpart in the generated code).
+ * nsys systems (T - eps_s) x_s = b_s on periodic n^3 grids (n a multiple of
+ * 8) with grid spacings h[3], T the 3D kinetic operator (kinetic sweeps of
+ * the thread's compute mode), eps_s < 0; vectors are device float64 arrays
+ * of nsys * n^3 values, eps a device array of nsys values.
+ * --------------------------------------------------------------------- */
+/* Weights of the learned preconditioner (device pointers): four 3x3x3
+ * convolutions, wt[l] bfloat16 [27][16 cout][16 cin] (tap t = (dx+1) +
+ * 3(dy+1) + 9(dz+1)), bias[l] float [16]; input channels (r / s, eps),
+ * output channel 0; s = rms(r) per system; ReLU after layers 0-2. */
+typedef struct {
+    const void *wt[4];
+    const float *bias[4];
+} libconv_cnn_weights;
+/* y = (T - eps) x for every system. */
+int libconv_cg_apply(int n, int nsys, const double *h, const double *eps, const double *x,
+                     double *y, void *stream);
+/* x = solution from x0 = 0 by Jacobi-preconditioned CG (w == NULL) or by
+ * flexible CG preconditioned with z = s M(r / s, eps) (w != NULL); a system
+ * stops at ||r|| <= tol ||b||, or with LIBCONV_ENUMERIC when its residual
+ * becomes non-finite.  iters (host, nsys or NULL): iteration of
+ * convergence (maxit + 1 if not reached); res (host, nsys or NULL): the
+ * true residual norm ||b - (T - eps) x|| recomputed with the FP64 operator;
+ * fell_back (host, nsys or NULL): the iteration at which a system left the
+ * learned preconditioner for the plain one (its residual norm did not halve
+ * over 10 iterations), 0 if it never did. */
+int libconv_cg_solve(int n, int nsys, const double *h, const double *eps, const double *b,
+                     double *x, double tol, int maxit, const libconv_cnn_weights *w, int *iters,
+                     double *res, int *fell_back, void *stream);
+/* One 3x3x3 periodic convolution layer of the network over nsys n^3 grids.
+ * src_kind 0: 16-channel bfloat16 activations [sys][z][y][x][16];
+ *          1: float64 field times src_fac[s], with eps[s] as channel 1;
+ *          2: float64 field times src_fac[s] (single channel).
+ * dst_kind 0: bfloat16 activations relu(conv + bias);
+ *          1: float64 field dst_fac[s] (conv channel 0 + bias[0]);
+ *          2: bfloat16 activations conv, zeroed where mask (activations) <= 0.
+ * cout: output channels computed (<= 8: channels 0-7 only). */
+int libconv_cnn_conv(int n, int nsys, int src_kind, int dst_kind, const void *src,
+                     const double *src_fac, const double *eps, const void *wt, const float *bias,
+                     void *dst, const double *dst_fac, const void *mask, int cout, void *stream);
+/* Weight gradient of a layer: out[27*256 + 16] (float) = sum over points of
+ * g[p][cout] x[p + d_t][cin] ([27][16 cout][16 cin]) and of g[p][cout]
+ * (bias); g of kind 0 or 2, x of kind 0 or 1 (see libconv_cnn_conv); part:
+ * device scratch of libconv_cnn_wgrad_parts() * (27*256 + 16) floats. */
+int libconv_cnn_wgrad(int n, int nsys, int g_kind, const void *g, const double *g_fac, int x_kind,
+                      const void *x, const double *x_fac, const double *eps, float *part,
+                      float *out, void *stream);
+int libconv_cnn_wgrad_parts(int n, int nsys);
 
 #ifdef __cplusplus
 }
