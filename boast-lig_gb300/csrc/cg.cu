@@ -14,8 +14,9 @@
 //             M the 4-layer BF16 network of the conv kernels (cnn.cu).
 // A system stops updating once ||r_s|| <= tol ||b_s||; its iteration count
 // is the first iteration at which that held.
-// Fallback: a system whose residual norm fails to fall below kStallRatio of
-// its value kStallWindow iterations earlier switches to the plain (Jacobi)
+// Fallback: a system whose residual norm fails to fall below `ratio` times
+// its value `window` iterations earlier (libconv_cg_set_stall; default 0.5
+// and 10) switches to the plain (Jacobi)
 // preconditioner for the rest of its solve: z = jac r inside the same
 // recurrence, which is then exactly preconditioned CG (restarted with
 // beta = 0 at the switch).
@@ -34,8 +35,9 @@ namespace {
 
 constexpr int kBPS = 64;        // reduction blocks per system
 constexpr int kThreads = 256;
-constexpr int kStallWindow = 10;
-constexpr double kStallRatio = 0.5;
+// stagnation test of the learned phase (per calling thread)
+thread_local int t_stall_window = 10;
+thread_local double t_stall_ratio = 0.5;
 
 // Per-system partial sums of up to two inner products over a system's N
 // points; block (b, s) covers a contiguous chunk.
@@ -59,8 +61,13 @@ __device__ __forceinline__ void block_sum2(double v0, double v1, double *p0, dou
 // Ap = Tp - eps p; partials (p, Ap) and, when r is given, (p, r)
 __global__ void k_shift(const double *__restrict__ Tp, const double *__restrict__ p,
                         const double *__restrict__ eps, double *__restrict__ Ap,
-                        const double *__restrict__ r, double *part, double *part_pr, long long N) {
+                        const double *__restrict__ r, double *part, double *part_pr, long long N,
+                        const int *active) {
     const int s = blockIdx.y, b = blockIdx.x;
+    if (active && !active[s]) {                  // converged: nothing to update
+        if (threadIdx.x == 0) { part[s * kBPS + b] = 0.0; if (r) part_pr[s * kBPS + b] = 0.0; }
+        return;
+    }
     const long long lo = N * b / kBPS, hi = N * (b + 1) / kBPS, off = (long long)s * N;
     const double e = eps[s];
     double acc = 0.0, pr = 0.0;
@@ -77,8 +84,12 @@ __global__ void k_shift(const double *__restrict__ Tp, const double *__restrict_
 // x += alpha p; r -= alpha Ap; partial (r, r)
 __global__ void k_update(double *__restrict__ x, double *__restrict__ r, const double *__restrict__ p,
                          const double *__restrict__ Ap, const double *__restrict__ alpha, double *part,
-                         long long N) {
+                         long long N, const int *active) {
     const int s = blockIdx.y, b = blockIdx.x;
+    if (!active[s]) {                            // converged: x, r unchanged, (r, r) kept
+        if (threadIdx.x == 0) part[s * kBPS + b] = -1.0;
+        return;
+    }
     const long long lo = N * b / kBPS, hi = N * (b + 1) / kBPS, off = (long long)s * N;
     const double al = alpha[s];
     double acc = 0.0;
@@ -93,8 +104,13 @@ __global__ void k_update(double *__restrict__ x, double *__restrict__ r, const d
 
 // partials (z, r) and (z, Ap)
 __global__ void k_dot2(const double *__restrict__ z, const double *__restrict__ r,
-                       const double *__restrict__ Ap, double *p0, double *p1, long long N) {
+                       const double *__restrict__ Ap, double *p0, double *p1, long long N,
+                       const int *active = nullptr) {
     const int s = blockIdx.y, b = blockIdx.x;
+    if (active && !active[s]) {
+        if (threadIdx.x == 0) { p0[s * kBPS + b] = 0.0; p1[s * kBPS + b] = 0.0; }
+        return;
+    }
     const long long lo = N * b / kBPS, hi = N * (b + 1) / kBPS, off = (long long)s * N;
     double a = 0.0, c = 0.0;
     for (long long i = lo + threadIdx.x; i < hi; i += kThreads) {
@@ -108,8 +124,9 @@ __global__ void k_dot2(const double *__restrict__ z, const double *__restrict__ 
 // p = coef_s v + beta_s p   (coef = null: 1)
 __global__ void k_direction(double *__restrict__ p, const double *__restrict__ v,
                             const double *__restrict__ coef, const double *__restrict__ beta,
-                            long long N) {
+                            long long N, const int *active = nullptr) {
     const int s = blockIdx.y;
+    if (active && !active[s]) return;
     const long long off = (long long)s * N;
     const double c = coef ? coef[s] : 1.0, be = beta[s];
     for (long long i = (long long)blockIdx.x * kThreads + threadIdx.x; i < N;
@@ -156,23 +173,24 @@ __global__ void k_alpha(Scalars S, const double *pAp_part, const double *pr_part
 // after the update: rr, convergence, the preconditioner scale; plain CG also
 // forms beta (z = jac r, so (z, r) = jac rr)
 __global__ void k_after_update(Scalars S, const double *rr_part, int nsys, long long N, double tol,
-                               int it, int plain) {
+                               int it, int plain, int window, double ratio) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nsys) return;
+    if (!S.active[s]) return;                    // converged earlier: scalars frozen
     const double rr = sum_parts(rr_part, s);
     S.rr[s] = rr;
-    if (S.active[s] && !isfinite(rr)) {          // breakdown: stop, report -it
+    if (!isfinite(rr)) {          // breakdown: stop, report -it
         S.active[s] = 0;
         S.iters[s] = -it;
-    } else if (S.active[s] && sqrt(rr) <= tol * S.bnorm[s]) {
+    } else if (sqrt(rr) <= tol * S.bnorm[s]) {
         S.active[s] = 0;
         S.iters[s] = it;
     }
     const double sc = rr > 0.0 ? sqrt(rr / (double)N) : 1.0;
     S.scale[s] = sc;
     S.inv_scale[s] = 1.0 / sc;
-    if (!plain && it % kStallWindow == 0) {      // stagnation test of the learned phase
-        if (!S.fallback[s] && rr > kStallRatio * kStallRatio * S.rr_mark[s]) S.fallback[s] = it;
+    if (!plain && it % window == 0) {            // stagnation test of the learned phase
+        if (S.active[s] && !S.fallback[s] && rr > ratio * ratio * S.rr_mark[s]) S.fallback[s] = it;
         S.rr_mark[s] = rr;
     }
     if (plain) {
@@ -262,33 +280,42 @@ int ensure(Work &w, size_t bytes) {
 // A x for all systems: y = T x - eps x; pAp partials of (x, y)
 int apply_A(int n, int nsys, const double a[3], const double *eps, const double *x, double *y,
             double *w1, double *w2, double *Tx, double *part, cudaStream_t st,
-            const double *r_for_pr = nullptr, double *part_pr = nullptr) {
+            const double *r_for_pr = nullptr, double *part_pr = nullptr,
+            const int *active = nullptr) {
     const int dims[3] = {n, n, n}, bc[3] = {0, 0, 0};
     int rc = d_kin_narr_dev(3, dims, bc, nsys, x, Tx, w1, w2, a, 0.0, 0.0, st);
     if (rc) return rc;
     const long long N = (long long)n * n * n;
-    k_shift<<<dim3(kBPS, nsys), kThreads, 0, st>>>(Tx, x, eps, y, r_for_pr, part, part_pr, N);
+    k_shift<<<dim3(kBPS, nsys), kThreads, 0, st>>>(Tx, x, eps, y, r_for_pr, part, part_pr, N, active);
     return cudaGetLastError() == cudaSuccess ? LIBCONV_OK : lcg::report(LIBCONV_ECUDA, "k_shift launch");
 }
 
 // z = s M(r / s, eps): the four conv layers
 int precondition(int n, int nsys, const libconv_cnn_weights *W, const double *r, const double *eps,
                  const double *scale, const double *inv_scale, void *act1, void *act2, double *z,
-                 cudaStream_t st) {
+                 const int *active, cudaStream_t st) {
     int rc = libconv_cnn_conv(n, nsys, 1, 0, r, inv_scale, eps, W->wt[0], W->bias[0], act1, nullptr,
-                              nullptr, 16, st);
+                              nullptr, 16, active, st);
     if (!rc) rc = libconv_cnn_conv(n, nsys, 0, 0, act1, nullptr, nullptr, W->wt[1], W->bias[1], act2,
-                                   nullptr, nullptr, 16, st);
+                                   nullptr, nullptr, 16, active, st);
     if (!rc) rc = libconv_cnn_conv(n, nsys, 0, 0, act2, nullptr, nullptr, W->wt[2], W->bias[2], act1,
-                                   nullptr, nullptr, 16, st);
+                                   nullptr, nullptr, 16, active, st);
     if (!rc) rc = libconv_cnn_conv(n, nsys, 0, 1, act1, nullptr, nullptr, W->wt[3], W->bias[3], z,
-                                   scale, nullptr, 1, st);
+                                   scale, nullptr, 1, active, st);
     return rc ? lcg::report(rc, "preconditioner convolution failed") : LIBCONV_OK;
 }
 
 }  // namespace
 
 extern "C" {
+
+int libconv_cg_set_stall(int window, double ratio) {
+    if (window < 1 || !(ratio > 0.0) || ratio > 1.0)
+        return lcg::report(LIBCONV_EARG, "stall window must be >= 1 and ratio in (0, 1]");
+    t_stall_window = window;
+    t_stall_ratio = ratio;
+    return LIBCONV_OK;
+}
 
 int libconv_cg_apply(int n, int nsys, const double *h, const double *eps, const double *x, double *y,
                      void *stream) {
@@ -356,7 +383,8 @@ int libconv_cg_solve(int n, int nsys, const double *h, const double *eps, const 
     k_dot2<<<vgrid, kThreads, 0, st>>>(r, r, r, pa, pb, N);   // (b, b)
     k_init<<<sgrid, 128, 0, st>>>(S, pa, eps, dcoef, nsys, N);
     if (learned) {
-        if ((rc = precondition(n, nsys, W, r, eps, S.scale, S.inv_scale, act1, act2, z, st))) return rc;
+        if ((rc = precondition(n, nsys, W, r, eps, S.scale, S.inv_scale, act1, act2, z, nullptr, st)))
+            return rc;
         k_dot2<<<vgrid, kThreads, 0, st>>>(z, r, r, pa, pb, N);
         k_set_rz<<<sgrid, 128, 0, st>>>(S, pa, nsys);
         e = cudaMemcpyAsync(p, z, vec, cudaMemcpyDeviceToDevice, st);
@@ -366,25 +394,30 @@ int libconv_cg_solve(int n, int nsys, const double *h, const double *eps, const 
     }
     if (e != cudaSuccess) return lcg::report_cuda(e, "CG start");
 
-    std::vector<int> h_active(nsys);
+    std::vector<int> h_active(nsys), h_fb(nsys);
     int it = 0;
     const int check_every = 8;
+    bool use_net = learned;     // false once every active system is on the fallback
     while (it < maxit) {
         ++it;
         if ((rc = apply_A(n, nsys, a, eps, p, Ap, w1, w2, Tp, pa, st, learned ? r : nullptr,
-                          learned ? pe : nullptr)))
+                          learned ? pe : nullptr, S.active)))
             return rc;
         k_alpha<<<sgrid, 128, 0, st>>>(S, pa, learned ? pe : nullptr, nsys);
-        k_update<<<vgrid, kThreads, 0, st>>>(x, r, p, Ap, S.alpha, pb, N);
-        k_after_update<<<sgrid, 128, 0, st>>>(S, pb, nsys, N, tol, it, learned ? 0 : 1);
+        k_update<<<vgrid, kThreads, 0, st>>>(x, r, p, Ap, S.alpha, pb, N, S.active);
+        k_after_update<<<sgrid, 128, 0, st>>>(S, pb, nsys, N, tol, it, learned ? 0 : 1,
+                                              t_stall_window, t_stall_ratio);
         if (learned) {
-            if ((rc = precondition(n, nsys, W, r, eps, S.scale, S.inv_scale, act1, act2, z, st))) return rc;
+            if (use_net &&
+                (rc = precondition(n, nsys, W, r, eps, S.scale, S.inv_scale, act1, act2, z, S.active,
+                                   st)))
+                return rc;
             k_fallback_z<<<dim3(kBPS, nsys), kThreads, 0, st>>>(S, z, r, N);
-            k_dot2<<<vgrid, kThreads, 0, st>>>(z, r, Ap, pc, pd, N);
+            k_dot2<<<vgrid, kThreads, 0, st>>>(z, r, Ap, pc, pd, N, S.active);
             k_beta_fcg<<<sgrid, 128, 0, st>>>(S, pc, pd, nsys, it);
-            k_direction<<<dim3(kBPS, nsys), kThreads, 0, st>>>(p, z, nullptr, S.beta, N);
+            k_direction<<<dim3(kBPS, nsys), kThreads, 0, st>>>(p, z, nullptr, S.beta, N, S.active);
         } else {
-            k_direction<<<dim3(kBPS, nsys), kThreads, 0, st>>>(p, r, S.jac, S.beta, N);
+            k_direction<<<dim3(kBPS, nsys), kThreads, 0, st>>>(p, r, S.jac, S.beta, N, S.active);
         }
         e = cudaGetLastError();
         if (e != cudaSuccess) return lcg::report_cuda(e, "CG iteration launch");
@@ -395,6 +428,13 @@ int libconv_cg_solve(int n, int nsys, const double *h, const double *eps, const 
             bool any = false;
             for (int v : h_active) any |= v != 0;
             if (!any) break;
+            if (use_net) {   // the network is still needed by some active system?
+                e = cudaMemcpy(h_fb.data(), S.fallback, sizeof(int) * nsys, cudaMemcpyDeviceToHost);
+                if (e != cudaSuccess) return lcg::report_cuda(e, "CG fallback check");
+                bool need = false;
+                for (int s2 = 0; s2 < nsys; ++s2) need |= h_active[s2] && !h_fb[s2];
+                use_net = need;
+            }
         }
     }
     // iteration counts (maxit + 1 for systems that did not converge) and the

@@ -52,6 +52,7 @@ struct ConvArgs {
     const double *dst_fac;     // per system factor of DST_FIELD
     const __nv_bfloat16 *mask; // DST_ACT_MASK: keep where mask > 0
     int nout_tiles;            // 1 (cout 0-7) or 2 (cout 0-15)
+    const int *active;         // per system: 0 = skip its tiles (or null: all)
 };
 
 __device__ __forceinline__ uint32_t saddr(const void *p) {
@@ -139,6 +140,7 @@ __global__ void __launch_bounds__(kThreads) conv_kernel(const ConvArgs A) {
         const int s = (int)(tile / (tpa * tpa * tpa));
         const int tr = (int)(tile % (tpa * tpa * tpa));
         const int tx = (tr % tpa) * kT, ty = ((tr / tpa) % tpa) * kT, tz = (tr / (tpa * tpa)) * kT;
+        if (A.active && !A.active[s]) continue;   // uniform over the CTA
         __syncthreads();   // previous tile's halo fully consumed
         stage<SRC>(A, halo, s, tx - 1, ty - 1, tz - 1, kH, kH, kHalo);
         __syncthreads();
@@ -326,7 +328,8 @@ int libconv_cnn_wgrad_parts(int n, int nsys) {
 
 int libconv_cnn_conv(int n, int nsys, int src_kind, int dst_kind, const void *src, const double *src_fac,
                      const double *eps, const void *wt, const float *bias, void *dst,
-                     const double *dst_fac, const void *mask, int cout, void *stream) {
+                     const double *dst_fac, const void *mask, int cout, const int *active,
+                     void *stream) {
     if (check_common(n, nsys) || !src || !wt || !dst) return LIBCONV_EARG;
     ConvArgs A{};
     A.n = n;
@@ -342,6 +345,7 @@ int libconv_cnn_conv(int n, int nsys, int src_kind, int dst_kind, const void *sr
     A.dst_fac = dst_fac;
     A.mask = (const __nv_bfloat16 *)mask;
     A.nout_tiles = cout > 8 ? 2 : 1;
+    A.active = active;
     if ((src_kind != 0 && !src_fac) || (src_kind == 1 && !eps)) return LIBCONV_EARG;
     if ((dst_kind == 0 && !bias) || (dst_kind == 1 && (!dst_fac || !bias)) || (dst_kind == 2 && !mask))
         return LIBCONV_EARG;

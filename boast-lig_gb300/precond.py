@@ -38,10 +38,12 @@ def _bind():
         L.libconv_cg_solve.argtypes = [_int, _int, _D, _vp, _vp, _vp, _dbl, _int,
                                        ctypes.POINTER(_W), P, _D, P, _vp]
         L.libconv_cnn_conv.argtypes = [_int, _int, _int, _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
-                                       _vp, _int, _vp]
+                                       _vp, _int, _vp, _vp]
         L.libconv_cnn_wgrad.argtypes = [_int, _int, _int, _vp, _vp, _int, _vp, _vp, _vp, _vp, _vp,
                                         _vp]
         L.libconv_cnn_wgrad_parts.argtypes = [_int, _int]
+        L.libconv_cg_set_stall.argtypes = [_int, _dbl]
+        L.libconv_cg_set_stall.restype = _int
         for f in ('libconv_cg_apply', 'libconv_cg_solve', 'libconv_cnn_conv', 'libconv_cnn_wgrad',
                   'libconv_cnn_wgrad_parts'):
             getattr(L, f).restype = _int
@@ -69,6 +71,11 @@ def _check(st, name):
 
 
 # ---- solver entry points ------------------------------------------------------------
+def set_stall(window, ratio):
+    """Stagnation test of the learned phase (libconv_cg_set_stall)."""
+    _check(_bind().libconv_cg_set_stall(int(window), float(ratio)), 'libconv_cg_set_stall')
+
+
 def apply(n, eps, x, y, h, stream=None):
     """y = (T - eps) x for every system (device float64 tensors)."""
     L = _bind()
@@ -176,13 +183,13 @@ class Net:
         a1, a2, a3, u = ws['a1'], ws['a2'], ws['a3'], ws['u']
         s = _s(stream)
         _check(L.libconv_cnn_conv(n, nsys, 1, 0, _p(r), _p(fac), _p(eps), _p(wt[0]), _p(bias[0]),
-                                  _p(a1), None, None, 16, s), 'conv0')
+                                  _p(a1), None, None, 16, None, s), 'conv0')
         _check(L.libconv_cnn_conv(n, nsys, 0, 0, _p(a1), None, None, _p(wt[1]), _p(bias[1]), _p(a2),
-                                  None, None, 16, s), 'conv1')
+                                  None, None, 16, None, s), 'conv1')
         _check(L.libconv_cnn_conv(n, nsys, 0, 0, _p(a2), None, None, _p(wt[2]), _p(bias[2]), _p(a3),
-                                  None, None, 16, s), 'conv2')
+                                  None, None, 16, None, s), 'conv2')
         _check(L.libconv_cnn_conv(n, nsys, 0, 1, _p(a3), None, None, _p(wt[3]), _p(bias[3]), _p(u),
-                                  _p(one), None, 1, s), 'conv3')
+                                  _p(one), None, 1, None, s), 'conv3')
         return u
 
     def backward(self, n, r, eps, fac, g, ws, stream=None):
@@ -205,13 +212,13 @@ class Net:
 
         wgrad(3, 2, g, one, 0, a3, None, None)
         _check(L.libconv_cnn_conv(n, nsys, 2, 2, _p(g), _p(one), None, _p(wtd[3]), None, _p(ga),
-                                  None, _p(a3), 16, s), 'dgrad3')
+                                  None, _p(a3), 16, None, s), 'dgrad3')
         wgrad(2, 0, ga, None, 0, a2, None, None)
         _check(L.libconv_cnn_conv(n, nsys, 0, 2, _p(ga), None, None, _p(wtd[2]), None, _p(gb),
-                                  None, _p(a2), 16, s), 'dgrad2')
+                                  None, _p(a2), 16, None, s), 'dgrad2')
         wgrad(1, 0, gb, None, 0, a1, None, None)
         _check(L.libconv_cnn_conv(n, nsys, 0, 2, _p(gb), None, None, _p(wtd[1]), None, _p(ga),
-                                  None, _p(a1), 16, s), 'dgrad1')
+                                  None, _p(a1), 16, None, s), 'dgrad1')
         wgrad(0, 0, ga, None, 1, r, fac, eps)
         with torch.no_grad():
             for l in range(4):

@@ -302,8 +302,12 @@ int libconv_cg_apply(int n, int nsys, const double *h, const double *eps, const 
  * convergence (maxit + 1 if not reached); res (host, nsys or NULL): the
  * true residual norm ||b - (T - eps) x|| recomputed with the FP64 operator;
  * fell_back (host, nsys or NULL): the iteration at which a system left the
- * learned preconditioner for the plain one (its residual norm did not halve
- * over 10 iterations), 0 if it never did. */
+ * learned preconditioner for the plain one, 0 if it never did. */
+/* Stagnation test of the learned phase (calling thread): a system whose
+ * residual norm is above ratio times its value `window` iterations earlier
+ * (tested every `window` iterations) continues with the plain preconditioner
+ * (CG restarted from its current iterate).  Default 10 and 0.5. */
+int libconv_cg_set_stall(int window, double ratio);
 int libconv_cg_solve(int n, int nsys, const double *h, const double *eps, const double *b,
                      double *x, double tol, int maxit, const libconv_cnn_weights *w, int *iters,
                      double *res, int *fell_back, void *stream);
@@ -314,10 +318,12 @@ int libconv_cg_solve(int n, int nsys, const double *h, const double *eps, const 
  * dst_kind 0: bfloat16 activations relu(conv + bias);
  *          1: float64 field dst_fac[s] (conv channel 0 + bias[0]);
  *          2: bfloat16 activations conv, zeroed where mask (activations) <= 0.
- * cout: output channels computed (<= 8: channels 0-7 only). */
+ * cout: output channels computed (<= 8: channels 0-7 only); active (device,
+ * nsys ints, or NULL): systems with 0 are skipped (their output untouched). */
 int libconv_cnn_conv(int n, int nsys, int src_kind, int dst_kind, const void *src,
                      const double *src_fac, const double *eps, const void *wt, const float *bias,
-                     void *dst, const double *dst_fac, const void *mask, int cout, void *stream);
+                     void *dst, const double *dst_fac, const void *mask, int cout,
+                     const int *active, void *stream);
 /* Weight gradient of a layer: out[27*256 + 16] (float) = sum over points of
  * g[p][cout] x[p + d_t][cin] ([27][16 cout][16 cin]) and of g[p][cout]
  * (bias); g of kind 0 or 2, x of kind 0 or 1 (see libconv_cnn_conv); part:

@@ -67,12 +67,12 @@ def test_conv_forward_field_and_relu(pkg, P):
     fac = torch.full((nsys,), 2.0, dtype=torch.float64, device='cuda')
     z = torch.empty(nsys * n ** 3, dtype=torch.float64, device='cuda')
     assert L.libconv_cnn_conv(n, nsys, 0, 1, P._p(act), None, None, P._p(wt), P._p(bias), P._p(z),
-                              P._p(fac), None, 1, None) == 0
+                              P._p(fac), None, 1, None, None) == 0
     torch.cuda.synchronize()
     assert rel(z, 2.0 * ref[:, 0].reshape(-1).double()) <= 1e-4
     out = torch.empty_like(act)
     assert L.libconv_cnn_conv(n, nsys, 0, 0, P._p(act), None, None, P._p(wt), P._p(bias), P._p(out),
-                              None, None, 16, None) == 0
+                              None, None, 16, None, None) == 0
     torch.cuda.synchronize()
     want = torch.relu(ref).permute(0, 2, 3, 4, 1)
     assert rel(out.float(), want) <= 1.6e-2
@@ -93,7 +93,7 @@ def test_conv_field_input_with_eps_channel(pkg, P):
     ref = torch.relu(_conv_ref(_rnd(x), W, bias)).permute(0, 2, 3, 4, 1)
     out = torch.empty(nsys * n ** 3 * 16, dtype=torch.bfloat16, device='cuda')
     assert L.libconv_cnn_conv(n, nsys, 1, 0, P._p(r), P._p(fac), P._p(eps), P._p(wt), P._p(bias),
-                              P._p(out), None, None, 16, None) == 0
+                              P._p(out), None, None, 16, None, None) == 0
     torch.cuda.synchronize()
     assert rel(out.float().view(nsys, n, n, n, 16), ref) <= 1.6e-2
 
@@ -115,7 +115,7 @@ def test_input_and_weight_gradients(pkg, P):
     wtd = full.flip(0).transpose(1, 2).to(torch.bfloat16).contiguous()
     gin = torch.empty_like(act)
     assert L.libconv_cnn_conv(n, nsys, 0, 2, P._p(gout), None, None, P._p(wtd), None, P._p(gin),
-                              None, P._p(act), 16, None) == 0
+                              None, P._p(act), 16, None, None) == 0
     torch.cuda.synchronize()
     want = x.grad.permute(0, 2, 3, 4, 1) * (act.float() > 0)
     assert rel(gin.float(), want) <= 1.6e-2
