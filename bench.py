@@ -15,7 +15,7 @@ uniform [-1, 1], details uniform [-1, 1] x 1e-3) into 96^3, then analysis
 back; metric: 96^3 grid points per second through both transforms.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload mfkin128|wavelet96|orbitals512]
+                  [--workload mfkin128|wavelet96|orbitals512|precond256]
                   [--mode tc_exact|fp64|tc_bf16x3|tc_tf32x3]
 
 Workload orbitals512: 512 orbitals with axes uniform in {24..72} (seed 7),
@@ -23,6 +23,11 @@ Gaussian envelope times unit-RMS noise; MagicFilter3D free grow and
 Kinetic3D free per orbital, batched (one persistent launch per sweep stage,
 CUDA graph, autotuned); the line also times the same work as per-orbital
 calls of the single-grid entry points.
+
+Workload precond256: 256 shifted kinetic systems (T - eps) x = b on 48^3
+periodic grids (h = 0.4, eps uniform in [-1, -0.1], Gaussian-filtered
+noise right-hand sides with ||b|| = 1); metric: solves/s to ||r|| <= 1e-8 of
+flexible CG with the learned preconditioner, plain CG timed beside it.
 
 Modes: tc_exact (default) runs the tensor-core exact-digit sweeps (FP64
 accuracy); fp64 the FP64 FMA sweeps; tc_bf16x3 / tc_tf32x3 the split-precision
@@ -210,7 +215,74 @@ class Orbitals512:
         O.call('oracle_d_kin', 3, d, [2, 2, 2], x, tx, w1, w2, np.array(self.a), 0.0, 0.0)
 
 
-WORKLOADS = {'mfkin128': MfKin128(), 'wavelet96': Wavelet96(), 'orbitals512': Orbitals512()}
+class Precond256:
+    """256 shifted kinetic solves (T - eps) x = b on 48^3 periodic grids."""
+    name = 'precond256'
+    metric = ('solves/s to ||r|| <= 1e-8, 256 x 48^3 periodic (T - eps) x = b, flexible CG with '
+              'the learned preconditioner')
+    n = 48
+    h = 0.4
+    nsys = 256
+    tol = 1e-8
+    weights = 'precond_n48_h0.40.npz'
+
+    def systems(self):
+        package()
+        from boast_lig_gb300 import train_precond
+        return train_precond.test_systems(self.n, self.nsys, seed=11)
+
+
+def cpu_cg(O, n, h, eps, b, tol, maxit=3000):
+    """Plain (Jacobi) CG on the host with the oracle's kinetic operator; returns
+    the iteration count."""
+    N = b.size
+    a = np.array([-0.5 / h ** 2] * 3)
+    w1, w2, Ap = np.zeros(N), np.zeros(N), np.zeros(N)
+    x, r = np.zeros(N), b.copy()
+    p = r.copy()
+    rr = float(r @ r)
+    bn = np.sqrt(rr)
+    for it in range(1, maxit + 1):
+        O.call('oracle_d_kin', 3, [n] * 3, [0, 0, 0], p, Ap, w1, w2, a, -eps, 0.0)
+        al = rr / float(p @ Ap)
+        x += al * p
+        r -= al * Ap
+        rr_new = float(r @ r)
+        if np.sqrt(rr_new) <= tol * bn:
+            return it
+        p = r + (rr_new / rr) * p
+        rr = rr_new
+    return maxit + 1
+
+
+def cpu_solves(W, seconds):
+    """Plain CG solves of the benchmark systems on all host threads for about
+    `seconds`; returns (solves, time, threads)."""
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    O.lib()
+    b, eps = W.systems()
+    th = cpu_threads()
+    done = [0] * th
+    t0 = time.perf_counter()
+
+    def work(t):
+        s = t
+        while time.perf_counter() - t0 < seconds:
+            cpu_cg(O, W.n, W.h, float(eps[s % W.nsys]), b[s % W.nsys], W.tol)
+            done[t] += 1
+            s += th
+
+    ts = [threading.Thread(target=work, args=(t,)) for t in range(th)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    return sum(done), time.perf_counter() - t0, th
+
+
+WORKLOADS = {'mfkin128': MfKin128(), 'wavelet96': Wavelet96(), 'orbitals512': Orbitals512(),
+             'precond256': Precond256()}
 
 
 class Clocks:
@@ -346,6 +418,26 @@ def run_reference_orbitals(args, W):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_precond(args, W):
+    vals = []
+    for _ in range(max(args.steps, 1)):
+        k, t, th = cpu_solves(W, 10.0)
+        vals.append(k / t)
+    v = float(np.median(vals))
+    unit = 'solves/s'
+    line = {'impl': 'reference', 'metric': W.metric.replace('flexible CG with the learned '
+                                                            'preconditioner', 'plain CG on the host'),
+            'value': v, 'unit': unit, 'n_gpus': args.gpus, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': 1e3 / v, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded)',
+            'config': {'workload': f'plain CG (C oracle kinetic, numpy vector updates) on the '
+                                   f'256 benchmark systems, {th} host threads, ~10 s per step'},
+            'cpu_baseline': {'value': v, 'unit': unit, 'cores': th, 'kind': 'port',
+                             'sample': 'systems solved in ~10 s per step'},
+            'e2e': {'value': v, 'unit': unit, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get('RANK', '0'))
     if rank != 0:
@@ -353,6 +445,8 @@ def run_reference(args):
     W = WORKLOADS[args.workload]
     if W.name == 'orbitals512':
         return run_reference_orbitals(args, W)
+    if W.name == 'precond256':
+        return run_reference_precond(args, W)
     grids = W.base(4)
     th = cpu_threads()
     times, pts = cpu_run(W, grids, th, args.steps, max(args.warmup, 1))
@@ -541,12 +635,147 @@ def run_orbitals(args, W):
         dist.destroy_process_group()
 
 
+def run_precond(args, W):
+    """Batched solves: one step = the 256 systems solved by flexible CG with
+    the learned preconditioner (committed checkpoint) to ||r|| <= 1e-8;
+    plain (Jacobi) CG on the same systems timed beside it."""
+    import torch
+    pkg = package()
+    from boast_lig_gb300 import precond as P
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl', device_id=dev)
+    pkg.set_mode(getattr(pkg, MODES[args.mode if args.mode in ('fp64', 'tc_exact') else 'tc_exact']))
+    net = P.Net.load(os.path.join(P.WEIGHTS_DIR, W.weights), device=dev)
+    b_np, eps_np = W.systems()
+    n, h, nsys = W.n, [W.h] * 3, W.nsys
+    host_b = torch.from_numpy(b_np.reshape(-1)).pin_memory()
+    b = host_b.to(dev)
+    eps = torch.from_numpy(eps_np).to(dev)
+    x = torch.empty_like(b)
+    stream = torch.cuda.Stream(device=dev)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def timed(m, steps):
+        for _ in range(max(args.warmup, 3) if m is net else 1):
+            P.solve(n, eps, b, x, h, tol=W.tol, maxit=3000, net=m, stream=stream)
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            info = {}
+            it, res = P.solve(n, eps, b, x, h, tol=W.tol, maxit=3000, net=m, stream=stream,
+                              info=info)
+        e1.record(stream)
+        e1.synchronize()
+        barrier()
+        return e0.elapsed_time(e1), it, res, info
+
+    clocks = Clocks(local)
+    clocks.start()
+    ms, it, res, info = timed(net, args.steps)
+    ck = clocks.stop()
+    ms_plain, it_p, res_p, _ = timed(None, max(1, min(args.steps, 3)))
+    steps_plain = max(1, min(args.steps, 3))
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = t.item()
+    value = nsys * world * args.steps / (ms / 1e3)
+    plain = nsys * steps_plain / (ms_plain / 1e3)
+
+    # e2e: right-hand sides from pinned host memory, solutions back, every step
+    host_x = torch.empty(nsys * n ** 3, dtype=torch.float64).pin_memory()
+    t0 = time.perf_counter()
+    e_steps = max(2, min(args.steps, 5))
+    for _ in range(e_steps):
+        with torch.cuda.stream(stream):
+            b.copy_(host_b, non_blocking=True)
+        P.solve(n, eps, b, x, h, tol=W.tol, maxit=3000, net=net, stream=stream)
+        with torch.cuda.stream(stream):
+            host_x.copy_(x, non_blocking=True)
+        stream.synchronize()
+    e_t = (time.perf_counter() - t0) / e_steps
+    e2e = {'value': nsys * world / e_t, 'unit': 'solves/s', 'h2d_bytes_per_step': 8 * b.numel(),
+           'd2h_bytes_per_step': 8 * x.numel(),
+           'note': 'libconv_cg_solve (learned) with b copied in and x copied out from pinned '
+                   'host memory inside the timed region'}
+
+    # dominant kernel: one 16 -> 16 channel convolution layer over the batch
+    L = P._bind()
+    wt, _, bias = net._packed
+    a_in = torch.randn(nsys * n ** 3 * 16, device=dev).to(torch.bfloat16)
+    a_out = torch.empty_like(a_in)
+    sp = P._s(stream)
+    for _ in range(3):
+        L.libconv_cnn_conv(n, nsys, 0, 0, P._p(a_in), None, None, P._p(wt[1]), P._p(bias[1]),
+                           P._p(a_out), None, None, 16, None, sp)
+    c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    c0.record(stream)
+    for _ in range(10):
+        L.libconv_cnn_conv(n, nsys, 0, 0, P._p(a_in), None, None, P._p(wt[1]), P._p(bias[1]),
+                           P._p(a_out), None, None, 16, None, sp)
+    c1.record(stream)
+    c1.synchronize()
+    t_conv = c0.elapsed_time(c1) / 10 / 1e3
+    flops = nsys * n ** 3 * 16 * 16 * 27 * 2
+    pk = peaks()
+    achieved = flops / t_conv / 1e12
+    line = {'metric': W.metric, 'value': value, 'unit': 'solves/s', 'n_gpus': world,
+            'steps': args.steps, 'warmup': max(args.warmup, 3), 'ms_per_step': ms / args.steps,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f64 solver (vectors, inner products, scalars); bf16 network, fp32 accumulate',
+            'data': 'synthetic (seeded Gaussian-filtered noise right-hand sides, ||b|| = 1; eps '
+                    'uniform in [-1, -0.1])',
+            'config': {'workload': f'{nsys} systems of 48^3 periodic per GPU, h = 0.4, flexible '
+                                   'CG with the 4-layer 16-channel 3^3 network '
+                                   f'(weights/{W.weights}) to ||r|| <= 1e-8',
+                       'kinetic_mode': pkg.get_mode(),
+                       'iterations_mean': float(it.mean()), 'iterations_max': int(it.max()),
+                       'fell_back': int((info['fell_back'] > 0).sum()),
+                       'max_true_residual': float(res.max()),
+                       'plain_cg_solves_per_s': plain, 'plain_cg_iterations_mean': float(it_p.mean()),
+                       'plain_cg_iterations_max': int(it_p.max()),
+                       'plain_cg_max_true_residual': float(res_p.max()),
+                       'learned_over_plain': value / world / plain,
+                       'l2': 'working set (7 vectors x 226 MB + activations) far above L2'},
+            'clocks': ck, 'e2e': e2e, 'gpu_launches': args.steps * (15 * int(it.max()) + 12),
+            'roofline': {'bound': 'tensor', 'achieved': achieved, 'peak': pk['bf16'],
+                         'unit': 'TFLOP/s', 'frac': achieved / pk['bf16'], 'traffic': None,
+                         'kernel': 'conv_kernel<ACT,ACT_RELU> (16 -> 16 channels, 3^3, '
+                                   'mma.sync bf16, 256 x 48^3 points per launch)',
+                         'peak_source': pk['source'], 'launch_ms': t_conv * 1e3}}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        k, t, th = cpu_solves(W, 10.0)
+        line['cpu_baseline'] = {'value': k / t, 'unit': 'solves/s', 'cores': th, 'kind': 'port',
+                                'sample': f'{k} plain-CG solves in {t:.1f} s (C oracle kinetic), '
+                                          'one system per host thread at a time'}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
 def run_gpu(args):
     import torch
     pkg = package()
     W = WORKLOADS[args.workload]
     if W.name == 'orbitals512':
         return run_orbitals(args, W)
+    if W.name == 'precond256':
+        return run_precond(args, W)
     world = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
     local = int(os.environ.get('LOCAL_RANK', '0'))
