@@ -79,11 +79,12 @@ template <int KIND, int NT, int SCH> struct Geom {
     static constexpr int CE = 16 / ESZ;                          // elements per core-matrix row
     static constexpr int MK = 32 / ESZ;                          // K of one MMA
     static constexpr int ND = SCH == SCH_EXACT ? (PROD > 16 ? 8 : 7) : SCH == SCH_BF16X3 ? 3 : 2;
-    static constexpr int ORD = SCH == SCH_EXACT ? ND : 1;        // accumulators per block
+    static constexpr int ORD = ND;                               // order accumulators per block
+    static constexpr int BN = 16 * ORD;                          // rows of the stacked filter
+    static constexpr int LBO_B = BN * 16;                        // its K-direction chunk stride
     static constexpr int A_PLANE = kM * KT * ESZ;
-    static constexpr int B_PLANE = 16 * KB * ESZ;
     static constexpr int A_BYTES = ND * A_PLANE;
-    static constexpr int B_BYTES = ND * B_PLANE;
+    static constexpr int B_BYTES = BN * KB * ESZ;
     static constexpr int AUX = 1024 + 3 * 4 * kM;                // barriers, slots, row exponents
     static constexpr int SMEM = A_BYTES + B_BYTES + AUX + 1024;
     static constexpr int HALF_COLS = 2 * ORD * 16;               // one TMEM half (2 blocks)
@@ -91,10 +92,12 @@ template <int KIND, int NT, int SCH> struct Geom {
     static_assert(2 * HALF_COLS <= 512, "TMEM columns");
     static_assert(SMEM <= 232448, "shared memory");
     // Instruction descriptor (kind::f16 / kind::tf32): D F32; A and B F16
-    // (exact), BF16 or TF32 (formats 0, 1, 2); both K-major; N = 16, M = 128.
+    // (exact), BF16 or TF32 (formats 0, 1, 2); both K-major; M = 128; N is
+    // added per MMA (idesc()).
     static constexpr uint32_t FMT = SCH == SCH_EXACT ? 0u : SCH == SCH_BF16X3 ? 1u : 2u;
-    static constexpr uint32_t IDESC = (1u << 4) | (FMT << 7) | (FMT << 10) | ((16u >> 3) << 17) |
-                                      ((uint32_t)(kM >> 4) << 24);
+    static constexpr uint32_t IDESC0 = (1u << 4) | (FMT << 7) | (FMT << 10) |
+                                       ((uint32_t)(kM >> 4) << 24);
+    static constexpr uint32_t idesc(int n) { return IDESC0 | ((uint32_t)(n >> 3) << 17); }
 };
 
 // ---- PTX wrappers ----------------------------------------------------------------
@@ -109,8 +112,9 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint3
            ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
 }
 
-template <uint32_t IDESC, bool TF32>
-__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t accum) {
+template <bool TF32>
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t IDESC,
+                                    uint32_t accum) {
     if (TF32)
         asm volatile(
             "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
@@ -269,13 +273,15 @@ __device__ __forceinline__ void split_f32(uint32_t f, uint32_t (&h)[SPLITS]) {
 }
 
 // Issue the MMAs of one TMEM half (output blocks 2h, 2h+1) of a tile.  The
-// exact scheme accumulates one order k = s + t per 16-column accumulator (the
-// first pair of an order overwrites it); the split schemes accumulate their
-// pairs (bfloat16: the 6 of order <= 2; tf32: hi.hi, hi.lo, lo.hi) into one.
-// Output block j starts 16 elements into the A planes; one MMA covers 32
-// bytes of K (two core matrices).  Descriptors are advanced by adding the
-// (16-byte unit) offset to the start-address field (addresses < 256 KB never
-// carry out of it).
+// filter planes t = 0..ORD-1 are stacked along N in one matrix (rows 16t + n),
+// and the ORD accumulators of a block (order k = s + t at columns 16k) are
+// contiguous in TMEM, so ONE MMA per data plane s covers all its pairs:
+// D = columns 16s.. of the block, N = 16 (ORD - s) (a prefix of the stacked
+// filter), giving pair (s, t) at order s + t.  The s = 0 MMA of the first K
+// step initialises every order.  Output block j starts 16 elements into the A
+// planes; one MMA covers 32 bytes of K (two core matrices).  Descriptors are
+// advanced by adding the (16-byte unit) offset to the start-address field
+// (addresses < 256 KB never carry out of it).
 template <int KIND, int NT, int SCH, int H>
 __device__ __forceinline__ void issue_half(uint32_t tmem, uint64_t a_desc0, uint64_t b_desc0) {
     using G = Geom<KIND, NT, SCH>;
@@ -285,32 +291,16 @@ __device__ __forceinline__ void issue_half(uint32_t tmem, uint64_t a_desc0, uint
     for (int jj = 0; jj < 2; ++jj) {
         const int j = 2 * H + jj;
         const int a_blk = (16 / G::CE) * j * 2048;
-        if (SCH == SCH_EXACT) {
 #pragma unroll
-            for (int k = 0; k < G::ORD; ++k) {
-                const uint32_t d = tmem + (uint32_t)(H * G::HALF_COLS + (jj * G::ORD + k) * 16);
-                constexpr int kTop = G::ND - 1;
+        for (int sd = 0; sd < G::ND; ++sd) {
+            const uint32_t d = tmem + (uint32_t)(H * G::HALF_COLS + (jj * G::ORD + sd) * 16);
+            const uint32_t id = G::idesc(16 * (G::ORD - sd));
 #pragma unroll
-                for (int s = (k > kTop ? k - kTop : 0); s <= (k < kTop ? k : kTop); ++s)
-#pragma unroll
-                    for (int ks = 0; ks < NKS; ++ks) {
-                        const uint64_t ad = a_desc0 + (uint64_t)((s * G::A_PLANE + a_blk + 2 * ks * 2048) >> 4);
-                        const uint64_t bd = b_desc0 + (uint64_t)(((k - s) * G::B_PLANE + 2 * ks * 256) >> 4);
-                        mma<G::IDESC, TF>(d, ad, bd, (s == (k > kTop ? k - kTop : 0) && ks == 0) ? 0u : 1u);
-                    }
+            for (int ks = 0; ks < NKS; ++ks) {
+                const uint64_t ad = a_desc0 + (uint64_t)((sd * G::A_PLANE + a_blk + 2 * ks * 2048) >> 4);
+                const uint64_t bd = b_desc0 + (uint64_t)((2 * ks * G::LBO_B) >> 4);
+                mma<TF>(d, ad, bd, id, (sd == 0 && ks == 0) ? 0u : 1u);
             }
-        } else {
-            const uint32_t d = tmem + (uint32_t)(H * G::HALF_COLS + jj * 16);
-            constexpr int NP = TF ? 3 : 6;
-            constexpr int PS[6] = {0, 0, 1, 0, 1, 2}, PT[6] = {0, 1, 0, 2, 1, 0};
-#pragma unroll
-            for (int i = 0; i < NP; ++i)
-#pragma unroll
-                for (int ks = 0; ks < NKS; ++ks) {
-                    const uint64_t ad = a_desc0 + (uint64_t)((PS[i] * G::A_PLANE + a_blk + 2 * ks * 2048) >> 4);
-                    const uint64_t bd = b_desc0 + (uint64_t)((PT[i] * G::B_PLANE + 2 * ks * 256) >> 4);
-                    mma<G::IDESC, TF>(d, ad, bd, (i == 0 && ks == 0) ? 0u : 1u);
-                }
         }
     }
 }
@@ -397,7 +387,8 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
         const int n = rem / G::KB, kk = rem % G::KB;
         const int ti = kk / NCH - n / NCH;
         const uint32_t v = (ti >= 0 && ti < NT) ? F.dig[t][filter_index<KIND>(n % NCH, kk % NCH) * NT + ti] : 0u;
-        uint8_t *b = B + t * G::B_PLANE + (kk / G::CE) * 256 + (n >> 3) * 128 + (n & 7) * 16 +
+        const int row = 16 * t + n;                      // stacked filter planes
+        uint8_t *b = B + (kk / G::CE) * G::LBO_B + (row >> 3) * 128 + (row & 7) * 16 +
                      (kk % G::CE) * G::ESZ;
         if (G::ESZ == 4) *(uint32_t *)b = v;
         else *(unsigned short *)b = (unsigned short)v;
@@ -410,7 +401,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
     bool alive = true;
 
     const uint64_t a_desc0 = umma_desc(saddr(A), 2048, 128);
-    const uint64_t b_desc0 = umma_desc(saddr(B), 256, 128);
+    const uint64_t b_desc0 = umma_desc(saddr(B), G::LBO_B, 128);
     if (warp < kProducers / 32) {
         // ============ producers: thread = (row, half of the row segment);
         // half-warps cover 16 consecutive rows, lanes 0-15 elements [0, KT/2),
@@ -659,8 +650,11 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                         Y += ((long long)lo + 128) >> 8;
                         out = nanrow ? __longlong_as_double(0x7FF8000000000000LL)
                                      : scale_pow2(__ll2double_rn(Y), se);
-                    } else {
-                        out = f32_to_f64(acc[0][n]);
+                    } else {                              // sum of the order accumulators
+                        float f = __uint_as_float(acc[0][n]);
+#pragma unroll
+                        for (int k = 1; k < G::ORD; ++k) f += __uint_as_float(acc[k][n]);
+                        out = f32_to_f64(__float_as_uint(f));
                     }
                     const long long pos = q - S.out_lo;
                     const long long off = KIND == KREC ? (long long)c + 2 * pos
