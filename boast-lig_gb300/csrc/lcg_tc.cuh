@@ -29,8 +29,12 @@ void tc_filter_split(const double *taps, int ntaps, double a, int sch, TcFilter 
 bool sweep_tc_supported(const Sweep &S);
 long long sweep_tc_blocks(const Sweep &S);
 // status (device int) is set non-zero if a tensor-core wait timed out.
-cudaError_t launch_sweep_tc(const Sweep &S, const TcFilter &F, int sch, int *status,
+// lineE (exact scheme, or null): device scratch of sweep_tc_lines(S) ints; the
+// largest exponent of each line is computed into it first (one read of the
+// input), so the tensor-core sweep reads its input once.
+cudaError_t launch_sweep_tc(const Sweep &S, const TcFilter &F, int sch, int *status, int *lineE,
                             cudaStream_t st);
+long long sweep_tc_lines(const Sweep &S);
 // Tiles of one sweep (the unit a batched launch numbers consecutively).
 long long sweep_tc_tiles(const Sweep &S);
 bool sweep_tc_batch_supported(int kind, int ntaps);
@@ -44,9 +48,12 @@ namespace tck {
 long long tile_count_for(const Sweep &S, int qp);
 int sm_count();
 // Per-scheme launchers (one translation unit each).
-cudaError_t launch_exact(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st);
-cudaError_t launch_bf16x3(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st);
-cudaError_t launch_tf32x3(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st);
+cudaError_t launch_exact(const Sweep &S, const TcFilter &F, int *status, const int *lineE,
+                          cudaStream_t st);
+cudaError_t launch_bf16x3(const Sweep &S, const TcFilter &F, int *status, const int *lineE,
+                          cudaStream_t st);
+cudaError_t launch_tf32x3(const Sweep &S, const TcFilter &F, int *status, const int *lineE,
+                          cudaStream_t st);
 cudaError_t launch_exact_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
                                int nsweeps, const TcFilter &F, int *status, cudaStream_t st);
 cudaError_t launch_bf16x3_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,

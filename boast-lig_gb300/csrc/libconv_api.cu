@@ -115,6 +115,7 @@ struct DevState {
     cudaStream_t stream = nullptr;   // stream of the host-pointer entry points
     DevBuf buf[6];                   // x, y, w1, w2, dot partials, dot scalar
     DevBuf scratch;                  // dot partials of the *_dev entry points
+    DevBuf lineexp;                  // per-line exponents of the exact tensor-core sweeps
     DevBuf dscalar;
     DevBuf status;                   // device status word (bounded waits)
 };
@@ -357,8 +358,8 @@ int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, do
 // ---- execution ------------------------------------------------------------------
 // Launch the plan's sweeps with bound device pointers.  dot_dev receives the
 // dot product (device) when the plan has one; `scratch` holds the partials.
-int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, double *dot_dev,
-             int *status, cudaStream_t st) {
+int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, DevBuf &lineexp,
+             double *dot_dev, int *status, cudaStream_t st) {
     if (!valid_mode(t_mode)) return fail(LIBCONV_EMODE, "unknown mode %d", t_mode);
     for (const PlanStep &ps : P.steps) {
         Sweep S = ps.S;
@@ -385,7 +386,13 @@ int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, double *dot_
             if (sch == SCH_EXACT) tc_filter_digits(h_ftab + S.ftab, flat, S.has_a ? S.a : 1.0, F);
             else tc_filter_split(h_ftab + S.ftab, flat, S.has_a ? S.a : 1.0, sch, F);
             S.has_a = 0;   // folded into the filter operands
-            e = launch_sweep_tc(S, F, sch, status, st);
+            int *lineE = nullptr;
+            if (sch == SCH_EXACT) {
+                int rc = ensure(lineexp, (size_t)sweep_tc_lines(S) * sizeof(int));
+                if (rc) return rc;
+                lineE = (int *)lineexp.p;
+            }
+            e = launch_sweep_tc(S, F, sch, status, lineE, st);
         } else {
             e = launch_sweep_fp64(S, st);
         }
@@ -410,7 +417,7 @@ int exec_dev(const Plan &P, const double *x, double *y, double *w1, double *w2, 
     int rc;
     DevState *s = dev_state(rc);
     if (!s) return rc;
-    return run_plan(P, bufs, s->scratch, dot_dev, (int *)s->status.p, (cudaStream_t)stream);
+    return run_plan(P, bufs, s->scratch, s->lineexp, dot_dev, (int *)s->status.p, (cudaStream_t)stream);
 }
 
 // Read and clear the device status word (after the work was synchronised).
@@ -446,7 +453,7 @@ int exec_host(const Plan &P, const double *x, double *y, double *dot_host) {
         e = cudaMemcpyAsync(bufs[B_Y], y, P.y_read * sizeof(double), cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) return cuda_fail(e, "copy y to device");
     }
-    rc = run_plan(P, bufs, s->scratch, P.has_dot ? (double *)s->dscalar.p : nullptr,
+    rc = run_plan(P, bufs, s->scratch, s->lineexp, P.has_dot ? (double *)s->dscalar.p : nullptr,
                   (int *)s->status.p, st);
     if (rc) return rc;
     e = cudaMemcpyAsync(y, bufs[B_Y], P.elems[B_Y] * sizeof(double), cudaMemcpyDeviceToHost, st);

@@ -32,7 +32,49 @@ long long tile_count_for(const Sweep &S, int qp) {
     return ((nlines + 127) / 128) * ((nq + qp - 1) / qp) * S.narr;
 }
 
+// Largest exponent field over the elements each line of S uses (positions
+// 0..plen-1 of every channel; ld padding is not read), one int per line of
+// every array.  Contiguous lines (nL == 1): a warp per line, lanes along the
+// line; strided lines: a thread per line, consecutive lines in a warp.
+__global__ void line_exp_kernel(const Sweep S, int plen, int *out) {
+    const int nchan = S.kind == KCONV ? 1 : 2;
+    const long long nlines = (long long)S.nL * S.nR, total = nlines * S.narr;
+    const long long pext = (long long)S.in_ext * nchan;
+    auto offset = [&](int e) -> long long {          // element e of the used run
+        if (S.kind == KCONV || S.kind == KDEC) return e;   // interleaved pairs: contiguous
+        return e < plen ? e : (long long)(e - plen) + S.in_ext;   // blocked channels
+    };
+    const long long *xb = reinterpret_cast<const long long *>(S.x);
+    const int count = plen * nchan;
+    if (S.nL == 1) {
+        const int lane = threadIdx.x & 31;
+        for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total;
+             w += ((long long)gridDim.x * blockDim.x) >> 5) {
+            const long long arr = w / nlines, r = w % nlines;
+            const long long *base = xb + arr * S.x_arr + pext * r;
+            int mx = 0;
+            for (int e = lane; e < count; e += 32)
+                mx = max(mx, (int)(((unsigned long long)base[offset(e)] >> 52) & 0x7FF));
+            for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            if (lane == 0) out[w] = mx;
+        }
+    } else {
+        for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+             t += (long long)gridDim.x * blockDim.x) {
+            const long long arr = t / nlines, g = t % nlines;
+            const long long l = g % S.nL, r = g / S.nL;
+            const long long *base = xb + arr * S.x_arr + l + (long long)S.nL * pext * r;
+            int mx = 0;
+            for (int e = 0; e < count; ++e)
+                mx = max(mx, (int)(((unsigned long long)base[offset(e) * S.nL] >> 52) & 0x7FF));
+            out[t] = mx;
+        }
+    }
+}
+
 }  // namespace tck
+
+long long sweep_tc_lines(const Sweep &S) { return (long long)S.nL * S.nR * S.narr; }
 
 bool sweep_tc_supported(const Sweep &S) {
     if (S.kind == KCONV) return S.ntaps == 16 || S.ntaps == 29;
@@ -125,11 +167,25 @@ cudaError_t launch_sweep_tc_batch(int kind, int ntaps, const Sweep *descs, const
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_sweep_tc(const Sweep &S, const TcFilter &F, int sch, int *status,
+cudaError_t launch_sweep_tc(const Sweep &S, const TcFilter &F, int sch, int *status, int *lineE,
                             cudaStream_t st) {
-    if (sch == SCH_EXACT) return tck::launch_exact(S, F, status, st);
-    if (sch == SCH_BF16X3) return tck::launch_bf16x3(S, F, status, st);
-    if (sch == SCH_TF32X3) return tck::launch_tf32x3(S, F, status, st);
+    if (sch == SCH_EXACT) {
+        if (lineE) {
+            // positions a line's outputs read: 0..n-1, or the whole shrink input
+            const int up = S.lowfil + S.ntaps - 1;
+            const int plen = S.bc == BC_SHRINK ? S.qhi + up - S.in_lo + 1 : S.n;
+            const long long total = sweep_tc_lines(S);
+            const long long threads = S.nL == 1 ? total * 32 : total;
+            const long long want = (threads + 255) / 256;
+            const int grid = (int)(want < 8LL * tck::sm_count() ? want : 8LL * tck::sm_count());
+            tck::line_exp_kernel<<<grid > 0 ? grid : 1, 256, 0, st>>>(S, plen, lineE);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
+        return tck::launch_exact(S, F, status, lineE, st);
+    }
+    if (sch == SCH_BF16X3) return tck::launch_bf16x3(S, F, status, nullptr, st);
+    if (sch == SCH_TF32X3) return tck::launch_tf32x3(S, F, status, nullptr, st);
     return cudaErrorInvalidValue;
 }
 

@@ -6,13 +6,14 @@
 namespace lcg {
 namespace tck {
 
-cudaError_t launch_exact(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st) {
-    if (S.kind == KCONV && S.ntaps == 16) return launch<KCONV, 16, SCH_EXACT>(S, F, status, st);
-    if (S.kind == KCONV && S.ntaps == 29) return launch<KCONV, 29, SCH_EXACT>(S, F, status, st);
-    if (S.kind == KDEC && S.ntaps == 8) return launch<KDEC, 8, SCH_EXACT>(S, F, status, st);
-    if (S.kind == KDEC && S.ntaps == 16) return launch<KDEC, 16, SCH_EXACT>(S, F, status, st);
-    if (S.kind == KREC && S.ntaps == 8) return launch<KREC, 8, SCH_EXACT>(S, F, status, st);
-    if (S.kind == KREC && S.ntaps == 16) return launch<KREC, 16, SCH_EXACT>(S, F, status, st);
+cudaError_t launch_exact(const Sweep &S, const TcFilter &F, int *status, const int *lineE,
+                          cudaStream_t st) {
+    if (S.kind == KCONV && S.ntaps == 16) return launch<KCONV, 16, SCH_EXACT>(S, F, status, lineE, st);
+    if (S.kind == KCONV && S.ntaps == 29) return launch<KCONV, 29, SCH_EXACT>(S, F, status, lineE, st);
+    if (S.kind == KDEC && S.ntaps == 8) return launch<KDEC, 8, SCH_EXACT>(S, F, status, lineE, st);
+    if (S.kind == KDEC && S.ntaps == 16) return launch<KDEC, 16, SCH_EXACT>(S, F, status, lineE, st);
+    if (S.kind == KREC && S.ntaps == 8) return launch<KREC, 8, SCH_EXACT>(S, F, status, lineE, st);
+    if (S.kind == KREC && S.ntaps == 16) return launch<KREC, 16, SCH_EXACT>(S, F, status, lineE, st);
     return cudaErrorInvalidValue;
 }
 

@@ -192,6 +192,16 @@ __device__ __forceinline__ double scale_pow2(double d, int se) {
     return ldexp(d, se);                                       // result outside the normal range
 }
 
+// Integer value of an FP32 accumulator (an exact integer): one FP32 add of
+// 1.5 * 2^23 leaves it in the low mantissa bits when |v| < 2^22 (ulp 1 in
+// [2^23, 2^24)); `big` records a larger magnitude (the caller then converts
+// with the conversion instruction, which runs on the narrow FP64 pipe here).
+__device__ __forceinline__ int acc_int(uint32_t u, bool &big) {
+    const float f = __uint_as_float(u);
+    big |= !(fabsf(f) < 4194304.0f);
+    return __float_as_int(f + 12582912.0f) - 0x4B400000;
+}
+
 // FP32 bits -> FP64 value, integer only (normal, zero, subnormal flushed, inf/nan).
 __device__ __forceinline__ double f32_to_f64(uint32_t f) {
     const uint32_t sgn = f >> 31, ex = (f >> 23) & 0xFF, man = f & 0x7FFFFF;
@@ -339,7 +349,8 @@ __device__ __forceinline__ TileLoc locate(const Sweep &S0, const Sweep *descs,
 template <int KIND, int NT, int SCH, bool BATCH>
 __global__ void __launch_bounds__(kThreads, 1)
 sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilter F, int *status,
-                const Sweep *__restrict__ descs, const long long *__restrict__ prefix, int nsweeps) {
+                const Sweep *__restrict__ descs, const long long *__restrict__ prefix, int nsweeps,
+                const int *__restrict__ lineE) {
     using G = Geom<KIND, NT, SCH>;
     constexpr int NCH = G::NCH;
     extern __shared__ uint8_t smem_raw[];
@@ -480,7 +491,11 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                 }
             };
             int mx = 0, E = 0;
-            if (SCH == SCH_EXACT) {
+            if (SCH == SCH_EXACT && lineE) {
+                // largest exponent field of the line (line_exp_kernel)
+                mx = valid ? lineE[(long long)arr * nlines + g] : 0;
+                E = (mx ? mx : 1) - 1022;
+            } else if (SCH == SCH_EXACT) {
 #pragma unroll
                 for (int c0 = 0; c0 < H / 8; c0 += 2) {          // 16 loads in flight
                     long long b0[8], b1[8];
@@ -498,10 +513,13 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                 mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
                 E = (mx ? mx : 1) - 1022;
             }
+            // software pipeline: the next chunk's loads are in flight while the
+            // current chunk is cut into digits
+            long long bits[8], nxt[8];
+            load8(0, bits);
 #pragma unroll 1
             for (int c = 0; c < H / 8; ++c) {
-                long long bits[8];
-                load8(c, bits);
+                if (c + 1 < H / 8) load8(c + 1, nxt);
                 // 8 elements = 8 / CE core-matrix chunks of 2048 bytes (128 rows)
                 const int off = (half * (H / 8) + c) * (8 / G::CE) * 2048 + (row >> 3) * 128 + (row & 7) * 16;
                 if (SCH == SCH_EXACT) {
@@ -544,6 +562,8 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                         *(uint4 *)(A + sd * G::A_PLANE + off + 2048) = make_uint4(h[4][sd], h[5][sd], h[6][sd], h[7][sd]);
                     }
                 }
+#pragma unroll
+                for (int e = 0; e < 8; ++e) bits[e] = nxt[e];
             }
             if (half == 0) rowE[row] = mx == 0x7FF ? 0x7FFFFFFF : E;
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
@@ -603,6 +623,20 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             double *__restrict__ y = S.y + (long long)arr * S.y_arr;
             const double *__restrict__ xa = S.x + (long long)arr * S.x_arr;
             const double *__restrict__ x2 = S.x2 ? S.x2 + (long long)arr * S.x_arr : nullptr;
+            // this row's output element (position p, channel c) sits at
+            // yrow + yps p + ycs c; its x2 partial at x2row + x2s q; its input
+            // at xrow + nL ps (row bases formed once per tile)
+            const long long ys = S.transpose ? S.nR : S.nL;
+            double *const yrow = S.transpose ? y + rr : y + l + (long long)S.nL * out_pext * rr;
+            const long long yps = KIND == KREC ? 2 * ys : ys;
+            const long long ycs = KIND == KREC ? ys : ys * S.out_ext;
+            const bool grow = S.bc == BC_GROW;
+            const double *const x2row = !x2 ? nullptr
+                : grow ? (S.transpose ? x2 + rr : x2 + l + (long long)S.nL * S.out_ext * rr)
+                       : x2 + l + (long long)S.nL * S.in_ext * rr;
+            const long long x2s = grow ? ys : S.nL;
+            const int x2lo = grow ? S.out_lo : S.in_lo;
+            const double *const xrow = xa + l + (long long)S.nL * S.in_ext * rr;
             const int se = Er + F.ef - 56;
             const bool nanrow = SCH == SCH_EXACT && Er == 0x7FFFFFFF;
 #pragma unroll 1
@@ -621,32 +655,37 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                 }
                 if (!valid) continue;
                 const int e0 = 16 * (2 * hf + jj) + n0;         // first output element of the step
+                const int q0 = qc0 + e0 / NCH;                  // e0 is a multiple of 8
+                const int nv = (S.qhi - q0 + 1) * NCH;          // valid elements of the step
+                double *const ystep = yrow + yps * (q0 - S.out_lo);
                 double add[8];
+                if (KIND == KCONV && x2) {
+                    const double *const x2step = x2row + x2s * (q0 - x2lo);
 #pragma unroll
-                for (int n = 0; n < 8; ++n) {
-                    add[n] = 0.0;
-                    const int q = qc0 + (e0 + n) / NCH;
-                    if (KIND == KCONV && x2 && q <= S.qhi) {
-                        const long long pos = q - S.out_lo;
-                        const long long x2i = S.bc == BC_GROW
-                            ? (S.transpose ? rr + (long long)S.nR * pos : l + (long long)S.nL * (pos + (long long)S.out_ext * rr))
-                            : l + (long long)S.nL * ((long long)(q - S.in_lo) + (long long)S.in_ext * rr);
-                        add[n] = x2[x2i];
-                    }
+                    for (int n = 0; n < 8; ++n) add[n] = n < nv ? x2step[x2s * n] : 0.0;
                 }
 #pragma unroll
                 for (int n = 0; n < 8; ++n) {
-                    const int q = qc0 + (e0 + n) / NCH, c = (e0 + n) % NCH;
-                    if (q > S.qhi) break;
+                    const int q = q0 + n / NCH, c = n % NCH;
+                    if (n >= nv) break;
                     double out;
                     if (SCH == SCH_EXACT) {
                         // Y = sum_{k<=5} Acc_k 2^(8(5-k)) + Acc_6 2^-8 (+ Acc_7 2^-16), Horner form
-                        long long Y = __float2int_rn(__uint_as_float(acc[0][n]));
+                        bool big = false;
+                        long long Y = acc_int(acc[0][n], big);
 #pragma unroll
-                        for (int k = 1; k < 6; ++k)
-                            Y = Y * 256 + __float2int_rn(__uint_as_float(acc[k][n]));
-                        int lo = __float2int_rn(__uint_as_float(acc[6][n]));
-                        if (G::ORD > 7) lo += (__float2int_rn(__uint_as_float(acc[G::ORD - 1][n])) + 128) >> 8;
+                        for (int k = 1; k < 6; ++k) Y = Y * 256 + acc_int(acc[k][n], big);
+                        int lo = acc_int(acc[6][n], big);
+                        if (G::ORD > 7) lo += (acc_int(acc[G::ORD - 1][n], big) + 128) >> 8;
+                        if (big) {                        // an accumulator >= 2^22: exact path
+                            Y = __float2int_rn(__uint_as_float(acc[0][n]));
+#pragma unroll
+                            for (int k = 1; k < 6; ++k)
+                                Y = Y * 256 + __float2int_rn(__uint_as_float(acc[k][n]));
+                            lo = __float2int_rn(__uint_as_float(acc[6][n]));
+                            if (G::ORD > 7)
+                                lo += (__float2int_rn(__uint_as_float(acc[G::ORD - 1][n])) + 128) >> 8;
+                        }
                         Y += ((long long)lo + 128) >> 8;
                         out = nanrow ? __longlong_as_double(0x7FF8000000000000LL)
                                      : scale_pow2(__ll2double_rn(Y), se);
@@ -656,23 +695,19 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                         for (int k = 1; k < G::ORD; ++k) f += __uint_as_float(acc[k][n]);
                         out = f32_to_f64(__float_as_uint(f));
                     }
-                    const long long pos = q - S.out_lo;
-                    const long long off = KIND == KREC ? (long long)c + 2 * pos
-                                                       : pos + (long long)S.out_ext * c;
-                    const long long yi = S.transpose ? rr + (long long)S.nR * off
-                                                     : l + (long long)S.nL * (off + out_pext * rr);
+                    double *const yp = ystep + yps * (n / NCH) + ycs * c;
                     if (KIND == KCONV) {
-                        if ((S.has_dot || S.has_ax) && (S.bc != BC_GROW || (q >= 0 && q < S.n))) {
+                        if ((S.has_dot || S.has_ax) && (!grow || (q >= 0 && q < S.n))) {
                             const int ps = S.bc == BC_PERIODIC ? imod(q, S.n) : q - S.in_lo;
-                            const double xq = xa[l + (long long)S.nL * ((long long)ps + (long long)S.in_ext * rr)];
+                            const double xq = xrow[(long long)S.nL * ps];
                             if (S.has_dot) dot = fma(xq, out, dot);
                             if (S.has_ax) out = fma(xq, S.a_x, out);
                         }
                         if (x2) out += add[n];
                     }
-                    if (S.ay_mode == 2) out += y[yi];
-                    else if (S.ay_mode == 1) out = fma(S.a_y, y[yi], out);
-                    y[yi] = out;
+                    if (S.ay_mode == 2) out += *yp;
+                    else if (S.ay_mode == 1) out = fma(S.a_y, *yp, out);
+                    *yp = out;
                 }
             }
         }
@@ -712,14 +747,15 @@ cudaError_t set_smem_attr() {
 }
 
 template <int KIND, int NT, int SCH>
-cudaError_t launch(const Sweep &S, const TcFilter &F, int *status, cudaStream_t st) {
+cudaError_t launch(const Sweep &S, const TcFilter &F, int *status, const int *lineE,
+                   cudaStream_t st) {
     using G = Geom<KIND, NT, SCH>;
     cudaError_t e = set_smem_attr<KIND, NT, SCH, false>();
     if (e != cudaSuccess) return e;
     const long long tiles = tile_count_for(S, G::QP);
     const int grid = (int)(tiles < sm_count() ? tiles : sm_count());
     sweep_tc_kernel<KIND, NT, SCH, false><<<grid, kThreads, G::SMEM, st>>>(S, F, status, nullptr,
-                                                                           nullptr, 0);
+                                                                           nullptr, 0, lineE);
     return cudaGetLastError();
 }
 
@@ -733,7 +769,7 @@ cudaError_t launch_batch(const Sweep *descs, const long long *prefix, int nsweep
     if (e != cudaSuccess) return e;
     Sweep S0{};
     sweep_tc_kernel<KIND, NT, SCH, true><<<sm_count(), kThreads, G::SMEM, st>>>(S0, F, status, descs,
-                                                                                prefix, nsweeps);
+                                                                                prefix, nsweeps, nullptr);
     return cudaGetLastError();
 }
 
