@@ -182,14 +182,29 @@ __device__ __forceinline__ int imod(int a, int n) {
     return r < 0 ? r + n : r;
 }
 
-// d * 2^se for an FP64 d produced from an integer (exact when the result is a
-// normal number: the exponent field is adjusted with one integer add).
-__device__ __forceinline__ double scale_pow2(double d, int se) {
-    const long long b = __double_as_longlong(d);
-    const int e = (int)((b >> 52) & 0x7FF);
-    if (e == 0) return d;                                      // zero
-    if (e + se >= 1 && e + se <= 2046) return __longlong_as_double(b + ((long long)se << 52));
-    return ldexp(d, se);                                       // result outside the normal range
+// Y * 2^se as an FP64, Y rounded to 53 bits to nearest-even (the rounding of
+// an int64 -> FP64 conversion), built from bits on the integer pipes: the
+// conversion instruction runs on the narrow FP64 pipe of this GPU.  ldexp
+// when the result is not a normal number.
+__device__ __forceinline__ double ll_scaled(long long Y, int se) {
+    if (Y == 0) return 0.0;
+    const unsigned long long sg = (unsigned long long)Y & 0x8000000000000000ull;
+    unsigned long long a = Y < 0 ? 0ull - (unsigned long long)Y : (unsigned long long)Y;
+    int e = 63 - __clzll((long long)a);                         // a in [2^e, 2^(e+1))
+    if (e <= 52) {
+        a <<= (52 - e);
+    } else {
+        const int sh = e - 52;                                  // 1..10
+        const unsigned long long rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        a >>= sh;
+        if (rem > half || (rem == half && (a & 1ull))) ++a;
+        if (a >> 53) { a >>= 1; ++e; }
+    }
+    const int be = e + 1023 + se;
+    const unsigned long long m = a & 0xFFFFFFFFFFFFFull;
+    if (be >= 1 && be <= 2046)
+        return __longlong_as_double((long long)(sg | ((unsigned long long)be << 52) | m));
+    return ldexp(__longlong_as_double((long long)(sg | (1075ull << 52) | m)), e - 52 + se);
 }
 
 // Integer value of an FP32 accumulator (an exact integer): one FP32 add of
@@ -688,7 +703,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                         }
                         Y += ((long long)lo + 128) >> 8;
                         out = nanrow ? __longlong_as_double(0x7FF8000000000000LL)
-                                     : scale_pow2(__ll2double_rn(Y), se);
+                                     : ll_scaled(Y, se);
                     } else {                              // sum of the order accumulators
                         float f = __uint_as_float(acc[0][n]);
 #pragma unroll
