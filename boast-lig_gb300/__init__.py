@@ -49,7 +49,7 @@ SIGNATURES = {
     'd_s0s1_1d_sym8': _WAV1D, 'd_s1s0_1d_sym8': _WAV1D,
     'd_s0s1_1d_symicomb8': _WAV1D, 'd_s1s0_1d_symicomb8': _WAV1D,
     'd_sfrf_ld_narr': _MDT, 'd_rfsf_ld_narr': _MDT,
-    'd_kin': _KIN, 'd_kin_narr': _KINN, 'd_dwt_sym8': _WMD, 'd_idwt_sym8': _WMD,
+    'd_kin': _KIN, 'd_kin_ekin': _KIN + [_vp], 'd_kin_narr': _KINN, 'd_dwt_sym8': _WMD, 'd_idwt_sym8': _WMD,
     'd_dwt_sym8_narr': _WMDN, 'd_idwt_sym8_narr': _WMDN,
 }
 COST_SIGNATURES = {

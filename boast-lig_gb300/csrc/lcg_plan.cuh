@@ -13,6 +13,7 @@ enum BufId { B_X = 0, B_Y = 1, B_W1 = 2, B_W2 = 3 };
 struct PlanStep {
     Sweep S;
     int src, dst, src2;   // buffer ids (src2 = -1 if no x2)
+    int dot_slot = 0;     // entry of the dot output this step's dot product goes to
 };
 
 struct Plan {
@@ -20,6 +21,7 @@ struct Plan {
     size_t elems[4] = {0, 0, 0, 0};   // elements each buffer must hold
     size_t y_read = 0;                // y is read (a_y != 0)
     int has_dot = 0;
+    int ndot = 1;                     // dot outputs (one per kinetic direction for ekin)
 };
 
 // 3D MagicFilter (sfrf_ld_narr, one grid).  order == nullptr: the reference's

@@ -304,7 +304,7 @@ int plan_md_n(const OpDef &op, int d, const int *n, const int *bc, const int *or
 // Multi-D kinetic, transpose = 0 (Kinetic2.rb:1068-1090), over narr grids
 // laid back to back (narr = 1 is the reference's Kinetic()).
 int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, double a_y,
-             Plan &P, int narr = 1, const int *order = nullptr) {
+             Plan &P, int narr = 1, const int *order = nullptr, bool ekin = false) {
     if (narr < 1 || narr > 65535) return fail(LIBCONV_EARG, "narr=%d out of [1,65535]", narr);
     if (d < 1 || d > 16) return fail(LIBCONV_EARG, "d=%d out of [1,16]", d);
     if (!n || !bc || !a) return fail(LIBCONV_EARG, "n/bc/a must not be null");
@@ -344,6 +344,8 @@ int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, do
         st.src = B_X;
         st.dst = t;
         st.src2 = k == 0 ? -1 : s;
+        st.S.has_dot = ekin ? 1 : 0;   // x . (a_i D2_i x), before a_x x and the partial sum
+        st.dot_slot = i;
         st.S.narr = narr;
         st.S.x_arr = st.S.y_arr = tot;
         need(P, B_X, tot * narr);
@@ -352,6 +354,8 @@ int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, do
         P.steps.push_back(st);
     }
     P.y_read = a_y != 0.0 ? tot * narr : 0;
+    P.has_dot = ekin ? 1 : 0;
+    P.ndot = ekin ? d : 1;
     return LIBCONV_OK;
 }
 
@@ -398,7 +402,7 @@ int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, DevBuf &line
         }
         if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
         if (S.has_dot) {
-            e = launch_dot_reduce(S.dot_part, nb, dot_dev, 0, st);
+            e = launch_dot_reduce(S.dot_part, nb, dot_dev + ps.dot_slot, 0, st);
             if (e != cudaSuccess) return cuda_fail(e, "dot reduction launch");
         }
     }
@@ -442,7 +446,7 @@ int exec_host(const Plan &P, const double *x, double *y, double *dot_host) {
     if (!s) return rc;
     for (int b = 0; b < 4; ++b)
         if (P.elems[b] && (rc = ensure(s->buf[b], P.elems[b] * sizeof(double)))) return rc;
-    if (P.has_dot && (rc = ensure(s->dscalar, sizeof(double)))) return rc;
+    if (P.has_dot && (rc = ensure(s->dscalar, sizeof(double) * P.ndot))) return rc;
     double *bufs[4];
     for (int b = 0; b < 4; ++b) bufs[b] = P.elems[b] ? (double *)s->buf[b].p : nullptr;
     cudaStream_t st = s->stream;
@@ -459,7 +463,7 @@ int exec_host(const Plan &P, const double *x, double *y, double *dot_host) {
     e = cudaMemcpyAsync(y, bufs[B_Y], P.elems[B_Y] * sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e != cudaSuccess) return cuda_fail(e, "copy y to host");
     if (P.has_dot) {
-        e = cudaMemcpyAsync(dot_host, s->dscalar.p, sizeof(double), cudaMemcpyDeviceToHost, st);
+        e = cudaMemcpyAsync(dot_host, s->dscalar.p, sizeof(double) * P.ndot, cudaMemcpyDeviceToHost, st);
         if (e != cudaSuccess) return cuda_fail(e, "copy dot_in to host");
     }
     e = cudaStreamSynchronize(st);
@@ -731,6 +735,21 @@ int d_kin_dev(int d, const int *n, const int *bc, const double *x, double *y, do
     Plan P;
     int rc = plan_kin(d, n, bc, a, a_x, a_y, P);
     return rc ? rc : exec_dev(P, x, y, w1, w2, nullptr, stream);
+}
+
+int d_kin_ekin(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
+               double *w2, const double *a, double a_x, double a_y, double *kstrten) {
+    (void)w1; (void)w2;
+    Plan P;
+    int rc = plan_kin(d, n, bc, a, a_x, a_y, P, 1, nullptr, true);
+    return rc ? rc : exec_host(P, x, y, kstrten);
+}
+int d_kin_ekin_dev(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
+                   double *w2, const double *a, double a_x, double a_y, double *kstrten,
+                   void *stream) {
+    Plan P;
+    int rc = plan_kin(d, n, bc, a, a_x, a_y, P, 1, nullptr, true);
+    return rc ? rc : exec_dev(P, x, y, w1, w2, kstrten, stream);
 }
 
 int d_kin_narr(int d, const int *n, const int *bc, int narr, const double *x, double *y,

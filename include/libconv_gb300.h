@@ -178,6 +178,14 @@ int d_rfsf_ld_narr(int d, const int *n, const int *bc, const int *nx, const int 
  * Periodic and free (no-grow) boundaries. */
 int d_kin(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
           double *w2, const double *a, double a_x, double a_y);
+/* 3D kinetic with the kinetic energy of every direction:
+ * kinetic_per_ref_optim_ekin (BigDFT/Kinetic2.rb:21-112), generalised to the
+ * d_kin options.  y = sum_i a_i D2_i x + a_x x + a_y y as d_kin, and
+ * kstrten[i] = x . (a_i D2_i x) for each of the d directions (the reference's
+ * kstrten(1:3); with a_i = -0.5/h_i^2, a_x = 0, a_y = 1 it is that routine).
+ * kstrten: d doubles (host pointer here, device pointer for _dev). */
+int d_kin_ekin(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
+               double *w2, const double *a, double a_x, double a_y, double *kstrten);
 /* Extension (no counterpart in the generated code, which has no narr for
  * Kinetic()): the same 3D kinetic over narr grids laid back to back in x, y,
  * w1 and w2, in one launch per sweep. */
@@ -207,6 +215,9 @@ int d_rfsf_ld_narr_dev(int d, const int *n, const int *bc, const int *nx, const 
                        void *stream);
 int d_kin_dev(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
               double *w2, const double *a, double a_x, double a_y, void *stream);
+int d_kin_ekin_dev(int d, const int *n, const int *bc, const double *x, double *y, double *w1,
+                   double *w2, const double *a, double a_x, double a_y, double *kstrten,
+                   void *stream);
 int d_kin_narr_dev(int d, const int *n, const int *bc, int narr, const double *x, double *y,
                    double *w1, double *w2, const double *a, double a_x, double a_y, void *stream);
 int d_dwt_sym8_dev(int d, const int *n, const int *bc, const double *x, double *y, double *w1,

@@ -481,6 +481,43 @@ int oracle_d_idwt_sym8(int d, const int *n, const int *bc, const double *x, doub
  * Only size-preserving BCs (periodic, free no-grow): every sweep re-reads
  * the original x, so grow/shrink shapes cannot be chained.
  * ====================================================================== */
+/* kinetic_per_ref_optim_ekin (BigDFT/Kinetic2.rb:21-112, conv_kin_x/y/z
+ * 115-372): y += sum_d tt_d with tt_d = sum_l fil_d(l) x(.. i_d + l ..)
+ * (periodic, fil_d = -0.5/h_d^2 * D2), and kstrten[d] = sum tt_d * x, the
+ * kinetic energy of direction d.  Arrays 0:n_d-1 (the reference is called
+ * with n_d - 1 as its upper bound). */
+void oracle_kinetic_per_ref_ekin(int n1, int n2, int n3, const double *hgrid, const double *x,
+                                 double *y, double *kstrten)
+{
+    double fil[3][29];
+    for (int d = 0; d < 3; ++d) {
+        double scale = -0.5 / (hgrid[d] * hgrid[d]);
+        for (int i = 0; i <= 14; ++i) {
+            fil[d][14 + i] = LCG_KIN_FORTRAN[i] * scale;
+            fil[d][14 - i] = fil[d][14 + i];
+        }
+    }
+    const int n[3] = {n1, n2, n3};
+    for (int d = 0; d < 3; ++d) {
+        double ekin = 0.0;
+        for (int i3 = 0; i3 < n3; ++i3)
+            for (int i2 = 0; i2 < n2; ++i2)
+                for (int i1 = 0; i1 < n1; ++i1) {
+                    const int c[3] = {i1, i2, i3};
+                    double tt = 0.0;
+                    for (int l = -14; l <= 14; ++l) {
+                        int s[3] = {i1, i2, i3};
+                        s[d] = imod(c[d] + l, n[d]);
+                        tt = tt + x[s[0] + (size_t)n1 * (s[1] + (size_t)n2 * s[2])] * fil[d][l + 14];
+                    }
+                    const size_t k = i1 + (size_t)n1 * (i2 + (size_t)n2 * i3);
+                    y[k] = y[k] + tt;
+                    ekin = ekin + tt * x[k];
+                }
+        kstrten[d] = ekin;
+    }
+}
+
 int oracle_d_kin(int d, const int *n, const int *bc, const double *x, double *y,
                  double *w1, double *w2, const double *a, double a_x, double a_y)
 {

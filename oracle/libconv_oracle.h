@@ -68,6 +68,9 @@ int oracle_d_sfrf_ld_narr(int d, const int *n, const int *bc, const int *nx, con
                           int narr, const double *x, double *y, double *w1, double *w2);
 int oracle_d_rfsf_ld_narr(int d, const int *n, const int *bc, const int *nx, const int *ny,
                           int narr, const double *x, double *y, double *w1, double *w2);
+/* kinetic_per_ref_optim_ekin: y += T x, kstrten[d] = x . (T_d x) */
+void oracle_kinetic_per_ref_ekin(int n1, int n2, int n3, const double *hgrid, const double *x,
+                                 double *y, double *kstrten);
 int oracle_d_kin(int d, const int *n, const int *bc, const double *x, double *y,
                  double *w1, double *w2, const double *a, double a_x, double a_y);
 int oracle_d_dwt_sym8(int d, const int *n, const int *bc, const double *x, double *y,

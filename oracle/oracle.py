@@ -28,6 +28,7 @@ _SIGS = {
     'oracle_magicfilter_free_ref': [_int, _int, _D, _D],
     'oracle_magicfilter_free_t_ref': [_int, _int, _D, _D],
     'oracle_kinetic_per_ref': [_int, _int, _int, _D, _D, _D, _dbl],
+    'oracle_kinetic_per_ref_ekin': [_int, _int, _int, _D, _D, _D, _D],
     'oracle_synthesis_per_ref': [_int, _int, _D, _D],
     'oracle_synthesis_free_ref': [_int, _int, _D, _D],
     'oracle_analysis_per_ref': [_int, _int, _D, _D],

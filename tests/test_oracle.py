@@ -303,3 +303,28 @@ def test_oracle_rejects_bad_arguments(O, pkg):
     assert O.call('oracle_d_s0s0_1d_sym8_md', 1, 0, [8], 7, [8], [8], 1, x, y, 1.0, 0.0, 0.0) == -2
     assert O.call('oracle_d_s0s0_1d_sym8_md', 1, 0, [8], 1, [8], [8], 1, x, y, 1.0, 0.0, 0.0) == -3
     assert O.call('oracle_d_s0s0_1d_sym8_md', 1, 2, [8], 0, [8], [8], 1, x, y, 1.0, 0.0, 0.0) == -1
+
+
+def test_kinetic_ekin_restatement(O):
+    """kinetic_per_ref_optim_ekin (Kinetic2.rb:21-112): y += T x, and
+    kstrten(d) is the energy x . (T_d x) of direction d -- the same numbers as
+    kinetic_per_ref for y and as the generated 1D kinetic sweep with dot_in
+    for each direction."""
+    n = [12, 10, 9]
+    N = int(np.prod(n))
+    h = np.array([0.45, 0.4, 0.5])
+    rng = np.random.default_rng(0)
+    x, y = rng.standard_normal(N), rng.standard_normal(N)
+    y0 = y.copy()
+    k = np.zeros(3)
+    O.call('oracle_kinetic_per_ref_ekin', *n, h, x, y, k)
+    r = np.zeros(N)
+    O.call('oracle_kinetic_per_ref', *n, h, x, r, 0.0)
+    assert np.abs(y - (y0 + r)).max() <= 1e-13 * np.abs(r).max()
+    for d in range(3):
+        yd, dd = np.zeros(N), ctypes.c_double(0.0)
+        O.call('oracle_d_s0s0_1d_sym8_d2_dotin', 3, d, n, 0, n, n, 1, x, yd, -0.5 / h[d] ** 2,
+               0.0, 0.0, ctypes.pointer(dd))
+        assert abs(k[d] - dd.value) <= 1e-13 * abs(k[d])
+    # the energies add up to x . (T x)
+    assert abs(k.sum() - float(x @ r)) <= 1e-12 * abs(k.sum())

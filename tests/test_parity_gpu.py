@@ -327,3 +327,59 @@ def test_wavelet3d_narr_extension(pkg, O, bcs):
             assert O.call('oracle_' + op, 3, n, bcs, x[j * Ni:(j + 1) * Ni].copy(), yo,
                           np.zeros(big), np.zeros(big)) == 0
             assert rel(yg[j * No:(j + 1) * No], yo) <= TOL, (op, j)
+
+
+def test_kinetic_ekin_matches_reference_form(pkg, O):
+    """d_kin_ekin with a = -0.5/h^2, a_x = 0, a_y = 1 is
+    kinetic_per_ref_optim_ekin: y += T x and kstrten per direction."""
+    n = [24, 20, 18]
+    N = int(np.prod(n))
+    h = [0.45, 0.4, 0.5]
+    x, y0 = seeded(40, N), seeded(41, N)
+    yg, k = y0.copy(), np.zeros(3)
+    pkg.Kernel('d_kin_ekin').run(3, n, [0, 0, 0], x, yg, np.zeros(1), np.zeros(1),
+                                 [-0.5 / v ** 2 for v in h], 0.0, 1.0, k)
+    yo, ko = y0.copy(), np.zeros(3)
+    O.call('oracle_kinetic_per_ref_ekin', *n, np.array(h), x, yo, ko)
+    assert rel(yg, yo) <= TOL
+    assert np.abs(k - ko).max() <= TOL * np.abs(ko).max()
+
+
+@pytest.mark.parametrize('bcs', [[2, 2, 2], [0, 2, 0]])
+def test_kinetic_ekin_general_options(pkg, O, bcs):
+    """Free / mixed BCs with a_x and a_y: y as d_kin, kstrten[i] as the 1D
+    kinetic sweep with dot_in along axis i."""
+    n = [17, 13, 11]
+    N = int(np.prod(n))
+    a = [-2.2, -1.7, -3.1]
+    x, y0 = seeded(42, N), seeded(43, N)
+    yg, k = y0.copy(), np.zeros(3)
+    pkg.Kernel('d_kin_ekin').run(3, n, bcs, x, yg, np.zeros(1), np.zeros(1), a, 0.3, -0.7, k)
+    yo = y0.copy()
+    assert O.call('oracle_d_kin', 3, n, bcs, x, yo, np.zeros(N), np.zeros(N), np.array(a), 0.3,
+                  -0.7) == 0
+    assert rel(yg, yo) <= TOL
+    for i in range(3):
+        yd, dd = np.zeros(N), ctypes.c_double(0.0)
+        assert O.call('oracle_d_s0s0_1d_sym8_d2_dotin', 3, i, n, bcs[i], n, n, 1, x, yd, a[i], 0.0,
+                      0.0, ctypes.pointer(dd)) == 0
+        assert abs(k[i] - dd.value) <= 1e-12 * abs(dd.value), (i, k[i], dd.value)
+
+
+def test_kinetic_ekin_device_entry(pkg, O):
+    import torch
+    n = [16, 24, 20]
+    N = int(np.prod(n))
+    x = seeded(44, N)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.zeros(N, dtype=torch.float64, device='cuda')
+    w1, w2 = torch.empty_like(yd), torch.empty_like(yd)
+    kd = torch.zeros(3, dtype=torch.float64, device='cuda')
+    h = [0.45] * 3
+    pkg.Kernel('d_kin_ekin').run_dev(3, n, [0, 0, 0], xd, yd, w1, w2, [-0.5 / v ** 2 for v in h],
+                                     0.0, 1.0, kd)
+    torch.cuda.synchronize()
+    yo, ko = np.zeros(N), np.zeros(3)
+    O.call('oracle_kinetic_per_ref_ekin', *n, np.array(h), x, yo, ko)
+    assert rel(yd.cpu().numpy(), yo) <= TOL
+    assert np.abs(kd.cpu().numpy() - ko).max() <= TOL * np.abs(ko).max()
