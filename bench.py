@@ -914,7 +914,9 @@ def run_gpu(args):
                        'mode': args.mode,
                        'l2': f'inputs larger than L2 ({B * Ni * 8 / 1e6:.0f} MB per array)',
                        **{f'ms_{o}': t / args.steps for o, t in zip(W.ops, op_ms)}},
-            'clocks': ck, 'e2e': e2e, 'gpu_launches': args.steps * W.launches,
+            'clocks': ck, 'e2e': e2e,
+            # each exact tensor-core sweep is preceded by its line-exponent pass
+            'gpu_launches': args.steps * W.launches * (2 if args.mode == 'tc_exact' else 1),
             'roofline': roof}
     if accuracy:
         line['accuracy_max_rel_error'] = accuracy
