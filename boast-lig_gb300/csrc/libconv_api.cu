@@ -335,7 +335,7 @@ int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, do
         const bool last = k == d - 1;
         st.S.has_a = 1;
         st.S.a = a[i];
-        st.S.has_ax = k == 0;
+        st.S.has_ax = k == 0 && a_x != 0.0;   // as the 1D dispatcher: no a_x term when 0
         st.S.a_x = a_x;
         st.S.ay_mode = (last && a_y != 0.0) ? 1 : 0;
         st.S.a_y = a_y;
