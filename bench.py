@@ -15,7 +15,7 @@ uniform [-1, 1], details uniform [-1, 1] x 1e-3) into 96^3, then analysis
 back; metric: 96^3 grid points per second through both transforms.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload mfkin128|wavelet96|orbitals512|precond256]
+                  [--workload mfkin128|wavelet96|orbitals512|precond256|hamiltonian48]
                   [--mode tc_exact|fp64|tc_bf16x3|tc_tf32x3]
 
 Workload orbitals512: 512 orbitals with axes uniform in {24..72} (seed 7),
@@ -28,6 +28,11 @@ Workload precond256: 256 shifted kinetic systems (T - eps) x = b on 48^3
 periodic grids (h = 0.4, eps uniform in [-1, -0.1], Gaussian-filtered
 noise right-hand sides with ||b|| = 1); metric: solves/s to ||r|| <= 1e-8 of
 flexible CG with the learned preconditioner, plain CG timed beside it.
+
+Workload hamiltonian48: the local Hamiltonian of orbitals on a 48^3 coarse
+grid with free boundaries (libconv_hamiltonian_dev: idwt grow, MagicFilter
+grow, potential and density, inverse MagicFilter shrink, kinetic with the
+energies, dwt shrink), 32 orbitals per step; metric: orbitals/s.
 
 Modes: tc_exact (default) runs the tensor-core exact-digit sweeps (FP64
 accuracy); fp64 the FP64 FMA sweeps; tc_bf16x3 / tc_tf32x3 the split-precision
@@ -232,6 +237,42 @@ class Precond256:
         return train_precond.test_systems(self.n, self.nsys, seed=11)
 
 
+class Hamiltonian48:
+    """Local Hamiltonian of orbitals on a 48^3 coarse grid, free boundaries."""
+    name = 'hamiltonian48'
+    metric = ('orbitals/s, local Hamiltonian (idwt grow, MagicFilter grow, potential, inverse '
+              'MagicFilter shrink, kinetic + energies, dwt shrink), 48^3 coarse points, free BC')
+    n = [48, 48, 48]
+    bc = [2, 2, 2]
+    h = 0.4
+    a = [-0.5 / 0.4 ** 2] * 3
+
+    def orbital(self, seed):
+        """Wavelet coefficients of one orbital: unit-RMS Gaussian-filtered noise
+        in the scaling subband, details 1e-3 of it (as the wavelet96 input)."""
+        package()
+        from boast_lig_gb300 import inputs
+        c = inputs.gaussian_filtered_noise(seed, (96, 96, 96))
+        c[48:, :, :] *= 1e-3
+        c[:, 48:, :] *= 1e-3
+        c[:, :, 48:] *= 1e-3
+        return np.ascontiguousarray(c).ravel(order='F')
+
+    def potential(self, nreal):
+        """A smooth attractive well plus a seeded perturbation, on the real-space grid."""
+        g = int(round(nreal ** (1 / 3)))
+        r = (np.arange(g) - (g - 1) / 2.0) / g
+        X, Y, Z = np.meshgrid(r, r, r, indexing='ij')
+        v = -1.0 / np.sqrt(X ** 2 + Y ** 2 + Z ** 2 + 0.05)
+        rng = np.random.default_rng(17)
+        v = v + 0.01 * rng.standard_normal(v.shape)
+        return np.ascontiguousarray(v).ravel(order='F')
+
+    def cpu_work(self, O, x, pot, bufs):
+        hpsig, ek, ep = bufs
+        O.call('oracle_hamiltonian', self.n, self.bc, np.array(self.a), x, pot, None, hpsig, ek, ep)
+
+
 def cpu_cg(O, n, h, eps, b, tol, maxit=3000):
     """Plain (Jacobi) CG on the host with the oracle's kinetic operator; returns
     the iteration count."""
@@ -282,7 +323,7 @@ def cpu_solves(W, seconds):
 
 
 WORKLOADS = {'mfkin128': MfKin128(), 'wavelet96': Wavelet96(), 'orbitals512': Orbitals512(),
-             'precond256': Precond256()}
+             'precond256': Precond256(), 'hamiltonian48': Hamiltonian48()}
 
 
 class Clocks:
@@ -438,11 +479,65 @@ def run_reference_precond(args, W):
     print(json.dumps(line), flush=True)
 
 
+def cpu_hamiltonian(W, xs, pot, seconds):
+    """oracle_hamiltonian on orbitals taken round robin by all host threads
+    for about `seconds` (every thread finishes the orbital it started);
+    returns (orbitals, time, threads)."""
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    O.lib()
+    th = cpu_threads()
+    bufs = [(np.zeros(xs[0].size), np.zeros(3), np.zeros(1)) for _ in range(th)]
+    done = [0] * th
+    t0 = time.perf_counter()
+
+    def work(t):
+        g = t
+        while True:
+            W.cpu_work(O, xs[g % len(xs)], pot, bufs[t])
+            done[t] += 1
+            g += th
+            if time.perf_counter() - t0 >= seconds:
+                break
+
+    ts = [threading.Thread(target=work, args=(t,)) for t in range(th)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    return sum(done), time.perf_counter() - t0, th
+
+
+def run_reference_hamiltonian(args, W):
+    package()
+    xs = [W.orbital(3000 + i) for i in range(4)]
+    pot = W.potential(int(np.prod([2 * v + 29 for v in W.n])))
+    vals = []
+    for _ in range(max(args.steps, 1)):
+        k, t, th = cpu_hamiltonian(W, xs, pot, 10.0)
+        vals.append(k / t)
+    v = float(np.median(vals))
+    unit = 'orbitals/s'
+    line = {'impl': 'reference', 'metric': W.metric, 'value': v, 'unit': unit,
+            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': 1e3 / v, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded)',
+            'config': {'workload': f'oracle_hamiltonian (C restatement of the composed '
+                                   f'reference dispatchers), {th} host threads taking orbitals '
+                                   'round robin, ~10 s per step', 'grid': W.n, 'bc': 'free'},
+            'cpu_baseline': {'value': v, 'unit': unit, 'cores': th, 'kind': 'port',
+                             'sample': 'orbitals processed in ~10 s per step'},
+            'e2e': {'value': v, 'unit': unit, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get('RANK', '0'))
     if rank != 0:
         return
     W = WORKLOADS[args.workload]
+    if W.name == 'hamiltonian48':
+        return run_reference_hamiltonian(args, W)
     if W.name == 'orbitals512':
         return run_reference_orbitals(args, W)
     if W.name == 'precond256':
@@ -768,10 +863,157 @@ def run_precond(args, W):
         dist.destroy_process_group()
 
 
+def run_hamiltonian(args, W):
+    """Local Hamiltonian of B orbitals per GPU per step: rho zeroed, then one
+    libconv_hamiltonian_dev call per orbital on one stream (rho accumulated
+    over the orbitals, per-orbital energies kept on the device)."""
+    import torch
+    pkg = package()
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl', device_id=dev)
+    pkg.set_mode(getattr(pkg, MODES[args.mode]))
+    nsig, nreal, nwork = pkg.hamiltonian_sizes(W.n, W.bc)
+    B = args.grids
+    base = [W.orbital(3000 + i) for i in range(4)]
+    host_x = torch.empty(B * nsig, dtype=torch.float64, pin_memory=True)
+    hx = host_x.numpy()
+    for b in range(B):
+        hx[b * nsig:(b + 1) * nsig] = base[(b + rank) % 4] * (1.0 + 1e-3 * b)
+    pot = W.potential(nreal)
+    host_pot = torch.from_numpy(pot).pin_memory()
+    dx, dpot = host_x.to(dev), host_pot.to(dev)
+    dh = torch.empty_like(dx)
+    drho = torch.zeros(nreal, dtype=torch.float64, device=dev)
+    E = torch.zeros(B, 4, dtype=torch.float64, device=dev)
+    H = pkg.Hamiltonian(W.n, W.bc, W.a, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+
+    def step():
+        with torch.cuda.stream(stream):
+            drho.zero_()
+        for b in range(B):
+            sl = slice(b * nsig, (b + 1) * nsig)
+            H(dx[sl], dpot, dh[sl], drho, stream=sp, energies=E[b])
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    stream.synchronize()
+    pkg.check(sp)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    clocks = Clocks(local)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    start.record(stream)
+    for _ in range(args.steps):
+        step()
+    stop.record(stream)
+    stop.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    ck = clocks.stop()
+    pkg.check(sp)
+    ms = start.elapsed_time(stop)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = t.item()
+    value = B * world * args.steps / (ms / 1e3)
+    en = E.cpu().numpy()
+
+    # e2e: the host-pointer C-ABI per orbital (H2D of psig, pot and rho, D2H
+    # of hpsig, rho and the energies inside every call)
+    hpot = host_pot.numpy()
+    hrho = torch.zeros(nreal, dtype=torch.float64, pin_memory=True).numpy()
+    pkg.hamiltonian(W.n, W.bc, W.a, hx[:nsig], hpot, hrho)
+    barrier()
+    e_steps = max(1, min(args.steps, 2))
+    t0 = time.perf_counter()
+    for _ in range(e_steps):
+        hrho[:] = 0.0
+        for b in range(B):
+            pkg.hamiltonian(W.n, W.bc, W.a, hx[b * nsig:(b + 1) * nsig], hpot, hrho)
+    barrier()
+    e_t = (time.perf_counter() - t0) / e_steps
+    e2e = {'value': B * world / e_t, 'unit': 'orbitals/s',
+           'h2d_bytes_per_step': B * (nsig + 2 * nreal) * 8,
+           'd2h_bytes_per_step': B * (nsig + nreal + 4) * 8,
+           'note': 'libconv_hamiltonian (host pointers) once per orbital'}
+
+    # pipeline roofline: the bytes every sweep reads and writes (the
+    # composition as separate sweeps), per orbital, against the HBM peak;
+    # the intermediates of one orbital (about 80 MB) can stay in L2
+    n0 = [2 * v + 14 for v in W.n]
+    nr = [v + 15 for v in n0]
+    nf, nR = int(np.prod(n0)), int(np.prod(nr))
+    sweep_bytes = 0
+    for d0, d1 in ((W.n, n0), (n0, nr), (nr, n0), (n0, W.n)):
+        dims = [2 * v for v in d0] if d0 is W.n else list(d0)
+        out = [2 * v for v in d1] if d1 is W.n else list(d1)
+        for i in range(3):
+            cur_in = int(np.prod(dims))
+            dims[i] = out[i]
+            sweep_bytes += 8 * (cur_in + int(np.prod(dims)))
+    sweep_bytes += 8 * nf * (2 + 3 + 3)      # kinetic: x each sweep, x2 twice, y RMW in the last
+    sweep_bytes += 8 * nR * 4                # potential: psir RW, pot, rho RW
+    pk = peaks()
+    t_orb = ms / 1e3 / (args.steps * B)
+    achieved = sweep_bytes / t_orb / 1e9
+    min_bytes = 8 * (2 * nsig + 3 * nR)
+    roof = {'bound': 'hbm', 'achieved': achieved, 'peak': pk['hbm'], 'unit': 'GB/s',
+            'frac': achieved / pk['hbm'], 'traffic': None, 'peak_source': pk['source'],
+            'kernel': 'whole pipeline (15 sweeps + potential) per orbital',
+            'algorithmic_bytes_per_orbital': sweep_bytes,
+            'compulsory_bytes_per_orbital': min_bytes,
+            'compulsory_frac': min_bytes / t_orb / 1e9 / pk['hbm']}
+    exact = args.mode in ('fp64', 'tc_exact')
+    launches = H.LAUNCHES['exact' if args.mode == 'tc_exact' else 'other']
+    line = {'metric': W.metric, 'value': value, 'unit': 'orbitals/s', 'n_gpus': world,
+            'steps': args.steps, 'warmup': max(args.warmup, 3), 'ms_per_step': ms / args.steps,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f64' if exact else ('f64 in HBM, ' + args.mode[3:] + ' split on tensor cores'),
+            'data': 'synthetic (seeded)',
+            'config': {'workload': f'{B} orbitals per GPU per step, 48^3 coarse points (96^3 '
+                                   'coefficients), free BC: 110^3 fine and 125^3 real-space '
+                                   'points; one potential, rho accumulated',
+                       'mode': args.mode, 'orbitals_per_gpu': B,
+                       'l2': f'inputs larger than L2 ({B * nsig * 8 / 1e6:.0f} MB of psig)',
+                       'energies_orbital0': {'ekin': [float(v) for v in en[0, :3]],
+                                             'epot': float(en[0, 3])}},
+            'clocks': ck, 'e2e': e2e, 'gpu_launches': args.steps * B * launches,
+            'roofline': roof}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        k, t, th = cpu_hamiltonian(W, base, pot, 10.0)
+        line['cpu_baseline'] = {'value': k / t, 'unit': 'orbitals/s', 'cores': th, 'kind': 'port',
+                                'sample': f'{k} orbitals in {t:.1f} s, oracle_hamiltonian, one '
+                                          'orbital per host thread'}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
 def run_gpu(args):
     import torch
     pkg = package()
     W = WORKLOADS[args.workload]
+    if W.name == 'hamiltonian48':
+        return run_hamiltonian(args, W)
     if W.name == 'orbitals512':
         return run_orbitals(args, W)
     if W.name == 'precond256':

@@ -245,6 +245,89 @@ def cost(name, *args):
     return out.value
 
 
+# ---- local Hamiltonian of one orbital ---------------------------------------------
+def _ham_lib():
+    L = lib()
+    if not getattr(L, '_ham_bound', False):
+        L.libconv_hamiltonian_sizes.argtypes = [_I, _I, _L, _L, _L]
+        L.libconv_hamiltonian.argtypes = [_I, _I, _D, _vp, _vp, _vp, _vp, _D, _D]
+        L.libconv_hamiltonian_dev.argtypes = [_I, _I, _D, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
+        for f in (L.libconv_hamiltonian_sizes, L.libconv_hamiltonian, L.libconv_hamiltonian_dev):
+            f.restype = _int
+        L._ham_bound = True
+    return L
+
+
+def _dbls(v):
+    v = [float(t) for t in v]
+    return ctypes.cast((ctypes.c_double * len(v))(*v), _D)
+
+
+def hamiltonian_sizes(n, bc):
+    """(nsig, nreal, nwork): elements of psig/hpsig, of the real-space grid
+    (pot, rho) and of the device workspace of the local Hamiltonian."""
+    L = _ham_lib()
+    out = [ctypes.c_longlong(0) for _ in range(3)]
+    st = L.libconv_hamiltonian_sizes(_ints(n), _ints(bc), *[ctypes.byref(o) for o in out])
+    if st:
+        raise LibconvError(st, 'libconv_hamiltonian_sizes', last_error())
+    return tuple(o.value for o in out)
+
+
+def hamiltonian(n, bc, a_kin, psig, pot, rho=None):
+    """Local Hamiltonian of one orbital on host arrays (libconv_hamiltonian,
+    the pipeline of BigDFT/libconv.f90:248-294).  Returns (hpsig, ekin[3],
+    epot); rho, when given, is updated in place with psir**2."""
+    nsig, nreal, _ = hamiltonian_sizes(n, bc)
+    if psig.size != nsig or pot.size != nreal or (rho is not None and rho.size != nreal):
+        raise ValueError(f'psig needs {nsig} and pot/rho {nreal} elements')
+    hpsig = np.zeros(nsig)
+    ek = (ctypes.c_double * 3)()
+    ep = ctypes.c_double(0.0)
+    st = _ham_lib().libconv_hamiltonian(
+        _ints(n), _ints(bc), _dbls(a_kin), _host_ptr(psig, False), _host_ptr(pot, False),
+        _host_ptr(rho, True), _host_ptr(hpsig, True), ctypes.cast(ek, _D), ctypes.pointer(ep))
+    if st:
+        raise LibconvError(st, 'libconv_hamiltonian', last_error())
+    return hpsig, np.array(ek[:]), ep.value
+
+
+class Hamiltonian:
+    """Device form (libconv_hamiltonian_dev) with its workspace: call with
+    float64 CUDA tensors; returns the device tensor [ekin_x, ekin_y, ekin_z,
+    epot], enqueued on `stream` (no synchronisation)."""
+
+    def __init__(self, n, bc, a_kin, device='cuda'):
+        import torch
+        self.n, self.bc, self.a_kin = list(n), list(bc), [float(v) for v in a_kin]
+        self.nsig, self.nreal, nwork = hamiltonian_sizes(n, bc)
+        self.work = torch.empty(nwork, dtype=torch.float64, device=device)
+        self.energies = torch.zeros(4, dtype=torch.float64, device=device)
+
+    # kernel launches of one call: 15 sweeps (x2 in the exact tensor-core mode,
+    # whose sweeps each follow a line-exponent pass), the potential kernel and
+    # its reduction, and the three kinetic-energy reductions
+    LAUNCHES = {'exact': 35, 'other': 20}
+
+    def __call__(self, psig, pot, hpsig, rho=None, stream=None, energies=None):
+        """energies: optional device tensor of 4 doubles to receive
+        [ekin_x, ekin_y, ekin_z, epot] instead of the object's own buffer."""
+        en = self.energies if energies is None else energies
+        if en.numel() != 4:
+            raise ValueError('energies needs 4 elements')
+        if psig.numel() != self.nsig or hpsig.numel() != self.nsig or pot.numel() != self.nreal:
+            raise ValueError(f'psig/hpsig need {self.nsig} and pot {self.nreal} elements')
+        if rho is not None and rho.numel() != self.nreal:
+            raise ValueError(f'rho needs {self.nreal} elements')
+        st = _ham_lib().libconv_hamiltonian_dev(
+            _ints(self.n), _ints(self.bc), _dbls(self.a_kin), _dev_ptr(psig), _dev_ptr(pot),
+            _dev_ptr(rho), _dev_ptr(hpsig), _dev_ptr(en), _dev_ptr(self.work),
+            _stream_ptr(stream))
+        if st:
+            raise LibconvError(st, 'libconv_hamiltonian_dev', last_error())
+        return en
+
+
 # ---- batched operators over many uneven grids ------------------------------------
 BATCH_OP_MF, BATCH_OP_KIN = 0, 1
 ENGINE_FP64_Q64, ENGINE_FP64_Q32, ENGINE_TC = 0, 1, 2

@@ -49,5 +49,11 @@ cudaError_t launch_sweep_fp64_batch(int kind, int ntaps, int qc, const Sweep *de
 // Deterministic sum of `count` partials into *out (device), on `st`.
 cudaError_t launch_dot_reduce(const double *part, long long count, double *out, int accumulate,
                               cudaStream_t st);
+// Potential step of the local Hamiltonian on `count` real-space points:
+// rho += psir^2 (rho may be null), *epot = sum pot psir^2, psir = pot psir.
+// part holds potential_blocks(count, sms) partial sums.
+int potential_blocks(long long count, int sms);
+cudaError_t launch_potential(double *psir, const double *pot, double *rho, long long count,
+                             double *part, int nblocks, double *epot, cudaStream_t st);
 
 }  // namespace lcg

@@ -118,6 +118,8 @@ struct DevState {
     DevBuf lineexp;                  // per-line exponents of the exact tensor-core sweeps
     DevBuf dscalar;
     DevBuf status;                   // device status word (bounded waits)
+    DevBuf potpart;                  // partial sums of the potential energy
+    DevBuf hbuf;                     // staging of the host-pointer local Hamiltonian
 };
 
 std::mutex g_mu;
@@ -471,6 +473,77 @@ int exec_host(const Plan &P, const double *x, double *y, double *dot_host) {
     return read_status(*s);
 }
 
+// ---- local Hamiltonian (BigDFT/libconv.f90:248-294) -------------------------------
+// The reference's libconvw sketch composes the dispatchers on one orbital:
+// idwt (grow) -> MagicFilter (grow) -> density and potential -> inverse
+// MagicFilter (shrink) -> kinetic with dot, accumulated (no-grow, a_y = 1)
+// -> dwt (shrink).  Free axes take that grow/shrink chain; periodic axes are
+// periodic in every step.
+struct Ham {
+    Plan idwt, mf, imf, kin, dwt;
+    int n0[3], nr[3];      // fine-grid extents of psi_fscf / hpsi and of psir
+    size_t nsig = 0;       // elements of psig and hpsig
+    size_t nfscf = 0;      // elements of psi_fscf and hpsi
+    size_t nreal = 0;      // elements of psir, pot and rho
+    size_t nw = 0;         // elements of each ping-pong workspace (w1, w2)
+    size_t nwork() const { return 2 * nfscf + nreal + 2 * nw; }
+};
+
+int plan_ham(const int *n, const int *bc, const double *a_kin, Ham &H) {
+    if (!n || !bc || !a_kin) return fail(LIBCONV_EARG, "n/bc/a_kin must not be null");
+    int bw[3], bi[3], bk[3];
+    for (int i = 0; i < 3; ++i) {
+        if (n[i] < 1) return fail(LIBCONV_EARG, "n[%d]=%d", i, n[i]);
+        if (bc[i] != BC_PERIODIC && bc[i] != BC_FREE)
+            return fail(LIBCONV_EBC, "local Hamiltonian: bc[%d]=%d is neither periodic nor free",
+                        i, bc[i]);
+        const bool fr = bc[i] == BC_FREE;
+        bw[i] = fr ? BC_GROW : BC_PERIODIC;     // idwt and MagicFilter
+        bi[i] = fr ? BC_SHRINK : BC_PERIODIC;   // inverse MagicFilter and dwt
+        bk[i] = fr ? BC_FREE : BC_PERIODIC;     // kinetic (no growth)
+        if (n[i] > (1 << 28)) return fail(LIBCONV_EARG, "n[%d]=%d too large", i, n[i]);
+        H.n0[i] = 2 * need_out(OP_IWT, bw[i], n[i]);
+        H.nr[i] = need_out(OP_MD, bw[i], H.n0[i]);
+    }
+    int rc;
+    if ((rc = plan_md_t(OP_IWT, 3, n, bw, nullptr, nullptr, 1, H.idwt))) return rc;
+    if ((rc = plan_md_t(OP_MD, 3, H.n0, bw, nullptr, nullptr, 1, H.mf))) return rc;
+    if ((rc = plan_md_t(OP_IMD, 3, H.n0, bi, nullptr, nullptr, 1, H.imf))) return rc;
+    if ((rc = plan_kin(3, H.n0, bk, a_kin, 0.0, 1.0, H.kin, 1, nullptr, true))) return rc;
+    if ((rc = plan_md_t(OP_DWT, 3, n, bi, nullptr, nullptr, 1, H.dwt))) return rc;
+    H.nsig = 8ull * n[0] * n[1] * n[2];
+    H.nfscf = (size_t)H.n0[0] * H.n0[1] * H.n0[2];
+    H.nreal = (size_t)H.nr[0] * H.nr[1] * H.nr[2];
+    for (const Plan *P : {&H.idwt, &H.mf, &H.imf, &H.kin, &H.dwt})
+        for (int b : {B_W1, B_W2}) if (P->elems[b] > H.nw) H.nw = P->elems[b];
+    return LIBCONV_OK;
+}
+
+// Enqueue the pipeline on `st`.  work: H.nwork() doubles; energies: 4
+// doubles (ekin of the three directions, then epot), device pointers.
+int run_ham(const Ham &H, const double *psig, const double *pot, double *rho, double *hpsig,
+            double *work, double *energies, DevState &s, cudaStream_t st) {
+    double *fscf = work, *hpsi = fscf + H.nfscf, *psir = hpsi + H.nfscf;
+    double *w1 = psir + H.nreal, *w2 = w1 + H.nw;
+    int *status = (int *)s.status.p;
+    double *b_idwt[4] = {const_cast<double *>(psig), fscf, w1, w2};
+    int rc = run_plan(H.idwt, b_idwt, s.scratch, s.lineexp, nullptr, status, st);
+    if (rc) return rc;
+    double *b_mf[4] = {fscf, psir, w1, w2};
+    if ((rc = run_plan(H.mf, b_mf, s.scratch, s.lineexp, nullptr, status, st))) return rc;
+    const int nb = potential_blocks((long long)H.nreal, tck::sm_count());
+    if ((rc = ensure(s.potpart, (size_t)nb * sizeof(double)))) return rc;
+    cudaError_t e = launch_potential(psir, pot, rho, (long long)H.nreal, (double *)s.potpart.p, nb,
+                                     energies + 3, st);
+    if (e != cudaSuccess) return cuda_fail(e, "potential launch");
+    double *b_imf[4] = {psir, hpsi, w1, w2};
+    if ((rc = run_plan(H.imf, b_imf, s.scratch, s.lineexp, nullptr, status, st))) return rc;
+    double *b_kin[4] = {fscf, hpsi, w1, w2};
+    if ((rc = run_plan(H.kin, b_kin, s.scratch, s.lineexp, energies, status, st))) return rc;
+    double *b_dwt[4] = {hpsi, hpsig, w1, w2};
+    return run_plan(H.dwt, b_dwt, s.scratch, s.lineexp, nullptr, status, st);
+}
+
 // ---- cost model (GenericConvolution2.rb:1269-1276, 1525-1558, 1850-1932) ----
 int cost_1d(const OpDef &op, int d, int idim, const int *n, int bc, int narr, long long *cost) {
     if (!cost || !n || d < 1 || idim < 0 || idim >= d || narr < 1)
@@ -764,6 +837,68 @@ int d_kin_narr_dev(int d, const int *n, const int *bc, int narr, const double *x
     Plan P;
     int rc = plan_kin(d, n, bc, a, a_x, a_y, P, narr);
     return rc ? rc : exec_dev(P, x, y, w1, w2, nullptr, stream);
+}
+
+int libconv_hamiltonian_sizes(const int *n, const int *bc, long long *nsig, long long *nreal,
+                              long long *nwork) {
+    Ham H;
+    const double a1[3] = {1.0, 1.0, 1.0};
+    int rc = plan_ham(n, bc, a1, H);
+    if (rc) return rc;
+    if (nsig) *nsig = (long long)H.nsig;
+    if (nreal) *nreal = (long long)H.nreal;
+    if (nwork) *nwork = (long long)H.nwork();
+    return LIBCONV_OK;
+}
+
+int libconv_hamiltonian(const int *n, const int *bc, const double *a_kin, const double *psig,
+                        const double *pot, double *rho, double *hpsig, double *ekin, double *epot) {
+    if (!psig || !pot || !hpsig || !ekin || !epot)
+        return fail(LIBCONV_EARG, "psig/pot/hpsig/ekin/epot must not be null");
+    Ham H;
+    int rc = plan_ham(n, bc, a_kin, H);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(g_mu);
+    DevState *s = dev_state(rc);
+    if (!s) return rc;
+    const size_t nd = 2 * H.nsig + (rho ? 2 : 1) * H.nreal + H.nwork() + 4;
+    if ((rc = ensure(s->hbuf, nd * sizeof(double)))) return rc;
+    double *d_psig = (double *)s->hbuf.p, *d_hpsig = d_psig + H.nsig, *d_pot = d_hpsig + H.nsig;
+    double *d_rho = rho ? d_pot + H.nreal : nullptr;
+    double *d_work = d_pot + (rho ? 2 : 1) * H.nreal, *d_en = d_work + H.nwork();
+    cudaStream_t st = s->stream;
+    cudaError_t e = cudaMemcpyAsync(d_psig, psig, H.nsig * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_pot, pot, H.nreal * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && rho)
+        e = cudaMemcpyAsync(d_rho, rho, H.nreal * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "copy inputs to device");
+    if ((rc = run_ham(H, d_psig, d_pot, d_rho, d_hpsig, d_work, d_en, *s, st))) return rc;
+    double en[4];
+    e = cudaMemcpyAsync(hpsig, d_hpsig, H.nsig * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && rho)
+        e = cudaMemcpyAsync(rho, d_rho, H.nreal * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(en, d_en, sizeof en, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "copy outputs to host");
+    if ((rc = read_status(*s))) return rc;
+    for (int i = 0; i < 3; ++i) ekin[i] = en[i];
+    *epot = en[3];
+    return LIBCONV_OK;
+}
+
+int libconv_hamiltonian_dev(const int *n, const int *bc, const double *a_kin, const double *psig,
+                            const double *pot, double *rho, double *hpsig, double *energies,
+                            double *work, void *stream) {
+    if (!psig || !pot || !hpsig || !energies || !work)
+        return fail(LIBCONV_EARG, "psig/pot/hpsig/energies/work must not be null");
+    Ham H;
+    int rc = plan_ham(n, bc, a_kin, H);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(g_mu);
+    DevState *s = dev_state(rc);
+    if (!s) return rc;
+    return run_ham(H, psig, pot, rho, hpsig, work, energies, *s, (cudaStream_t)stream);
 }
 
 int d_s0s0_1d_sym8_md_cost(int d, int idim, const int *n, int bc, int narr, long long *cost) {

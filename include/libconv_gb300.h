@@ -230,6 +230,46 @@ int d_idwt_sym8_dev(int d, const int *n, const int *bc, const double *x, double 
                     double *w1, double *w2, void *stream);
 
 /* ---------------------------------------------------------------------
+ * Local Hamiltonian of one orbital: the pipeline of the libconvw module
+ * (BigDFT/libconv.f90:248-294; the reference leaves it as an unfinished
+ * subroutine body), composed of the operators above on one stream:
+ *   psi_fscf = idwt(psig)            s1s0_md     SYM8_LP   grow
+ *   psir     = MF(psi_fscf)          s0s0_md     SYM8_MD   grow
+ *   rho     += psir^2                (skipped when rho is NULL)
+ *   epot     = sum pot * psir^2
+ *   psir     = pot * psir
+ *   hpsi     = MI(psir)              s0s0_md     SYM8_MI   shrink
+ *   hpsi    += sum_i a_kin[i] D2_i psi_fscf, and per direction
+ *   ekin[i]  = psi_fscf . (a_kin[i] D2_i psi_fscf)
+ *                                    s0s0_1ds_dot SYM8_D2  no-grow, a_y = 1
+ *   hpsig    = dwt(hpsi)             s0s1_md     SYM8_LP   shrink
+ * Along an axis with bc[i] = LIBCONV_BC_FREE the steps use the grow/shrink
+ * boundaries shown; along an axis with LIBCONV_BC_PERIODIC every step is
+ * periodic.  n[3]: coarse points (wavelet pairs) per axis; psig and hpsig
+ * hold 2n[0] x 2n[1] x 2n[2] values laid out as d_idwt_sym8's input.  The
+ * fine grid of psi_fscf has 2n[i] + 14 points along a free axis (2n[i]
+ * periodic), and the real-space grid of psir, pot and rho 15 more along a
+ * free axis.  a_kin[i]: scale of the kinetic filter along axis i, as a[] of
+ * d_kin (-0.5/h_i^2 for BigDFT's kinetic energy on spacing h_i).  The
+ * calling thread's compute mode applies to every sweep.
+ * Extension: no generated procedure of the reference does this in one call.
+ * ------------------------------------------------------------------- */
+/* Element counts: psig/hpsig, the real-space grid (pot, rho), and the
+ * device workspace of libconv_hamiltonian_dev.  Any output may be NULL. */
+int libconv_hamiltonian_sizes(const int *n, const int *bc, long long *nsig, long long *nreal,
+                              long long *nwork);
+/* Host pointers; ekin: 3 doubles, epot: 1 double; rho is read and updated
+ * when not NULL. */
+int libconv_hamiltonian(const int *n, const int *bc, const double *a_kin, const double *psig,
+                        const double *pot, double *rho, double *hpsig, double *ekin,
+                        double *epot);
+/* Device pointers, enqueued on `stream`; energies: 4 doubles on the device
+ * (ekin[0..2], epot); work: nwork doubles. */
+int libconv_hamiltonian_dev(const int *n, const int *bc, const double *a_kin, const double *psig,
+                            const double *pot, double *rho, double *hpsig, double *energies,
+                            double *work, void *stream);
+
+/* ---------------------------------------------------------------------
  * Cost model (ConvolutionOperator1d#cost / GenericConvolutionOperator#cost,
  * BigDFT/GenericConvolution2.rb:1269-1276, 1850-1932): the flop count the
  * reference uses for every GFlop/s it prints (n * filter.cost * ndat per

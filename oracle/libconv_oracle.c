@@ -6,6 +6,7 @@
  */
 #include <stddef.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include "libconv_oracle.h"
 #include "../boast-lig_gb300/csrc/libconv_filters.h"
 
@@ -543,4 +544,59 @@ int oracle_d_kin(int d, const int *n, const int *bc, const double *x, double *y,
         conv1d(&F_D2, bc[i], &c);
     }
     return OK;
+}
+
+/* ======================================================================
+ * Local Hamiltonian of one orbital: the libconvw pipeline of
+ * BigDFT/libconv.f90:248-294, composed of the dispatchers above.
+ *   idwt        s1s0_md(dwt_fil, 3*[grow])              :258-260
+ *   MagicFilter s0s0_md(md_fil, 3*[grow])               :262-264
+ *   rho = rho + psir**2 ; psir = v*psir                 :266-271
+ *   inverse MF  s0s0_md(mi_fil, 3*[shrink])             :274-276
+ *   kinetic     s0s0_1ds_dot(kin_fil, 3*[nogrow], a_y=1):278-280
+ *   dwt         s0s1_md(dwt_fil, 3*[shrink])            :284-286
+ * Free axes take these boundaries; periodic axes are periodic in every
+ * step.  ekin[i] = psi_fscf . (a_kin[i] D2_i psi_fscf) is the 1D dot_in
+ * of the kinetic sweep along axis i; epot = sum psir * (v psir).
+ * ====================================================================== */
+int oracle_hamiltonian(const int *n, const int *bc, const double *a_kin, const double *psig,
+                       const double *pot, double *rho, double *hpsig, double *ekin, double *epot)
+{
+    if (!n || !bc || !a_kin || !psig || !pot || !hpsig || !ekin || !epot) return E_ARG;
+    int bw[3], bi[3], bk[3], n0[3], nr[3];
+    for (int i = 0; i < 3; ++i) {
+        if (n[i] < 1) return E_ARG;
+        if (bc[i] != BC_PERIODIC && bc[i] != BC_FREE) return E_BC;
+        const int fr = bc[i] == BC_FREE;
+        bw[i] = fr ? BC_GROW : BC_PERIODIC;
+        bi[i] = fr ? BC_SHRINK : BC_PERIODIC;
+        bk[i] = fr ? BC_FREE : BC_PERIODIC;
+        n0[i] = 2 * need_out(fr ? &F_IWT_GS : &F_IWT_P, bw[i], n[i]);
+        nr[i] = need_out(&F_MD, bw[i], n0[i]);
+    }
+    const size_t nf = (size_t)n0[0] * n0[1] * n0[2], nrl = (size_t)nr[0] * nr[1] * nr[2];
+    double *fscf = malloc(nf * sizeof(double)), *hpsi = malloc(nf * sizeof(double));
+    double *tmp = malloc(nf * sizeof(double)), *psir = malloc(nrl * sizeof(double));
+    double *w1 = malloc(nrl * sizeof(double)), *w2 = malloc(nrl * sizeof(double));
+    int rc = (fscf && hpsi && tmp && psir && w1 && w2) ? OK : E_ARG;
+    if (rc == OK) rc = oracle_d_idwt_sym8(3, n, bw, psig, fscf, w1, w2);
+    if (rc == OK) rc = oracle_d_sfrf_ld_narr(3, n0, bw, 0, 0, 1, fscf, psir, w1, w2);
+    if (rc == OK) {
+        double ep = 0.0;
+        for (size_t k = 0; k < nrl; ++k) {
+            const double p = psir[k], hp = pot[k] * p;
+            if (rho) rho[k] = rho[k] + p * p;
+            ep = ep + p * hp;
+            psir[k] = hp;
+        }
+        *epot = ep;
+        rc = oracle_d_rfsf_ld_narr(3, n0, bi, 0, 0, 1, psir, hpsi, w1, w2);
+    }
+    if (rc == OK) rc = oracle_d_kin(3, n0, bk, fscf, hpsi, w1, w2, a_kin, 0.0, 1.0);
+    for (int i = 0; i < 3 && rc == OK; ++i)
+        rc = oracle_d_s0s0_1d_sym8_d2_dotin(3, i, n0, bk[i], n0, n0, 1, fscf, tmp, a_kin[i], 0.0,
+                                            0.0, &ekin[i]);
+    if (rc == OK) rc = oracle_d_dwt_sym8(3, n, bi, hpsi, hpsig, w1, w2);
+    free(fscf); free(hpsi); free(tmp); free(psir); free(w1); free(w2);
+    return rc;
 }

@@ -77,6 +77,12 @@ int oracle_d_dwt_sym8(int d, const int *n, const int *bc, const double *x, doubl
                       double *w1, double *w2);
 int oracle_d_idwt_sym8(int d, const int *n, const int *bc, const double *x, double *y,
                        double *w1, double *w2);
+/* Local Hamiltonian of one orbital (BigDFT/libconv.f90:248-294): idwt grow,
+ * MagicFilter grow, rho += psir^2 (rho may be NULL), epot = sum v psir^2,
+ * psir = v psir, inverse MagicFilter shrink, kinetic no-grow accumulated
+ * with ekin[3] per direction, dwt shrink.  bc[i]: periodic (0) or free (2). */
+int oracle_hamiltonian(const int *n, const int *bc, const double *a_kin, const double *psig,
+                       const double *pot, double *rho, double *hpsig, double *ekin, double *epot);
 
 #ifdef __cplusplus
 }

@@ -47,6 +47,7 @@ _SIGS['oracle_d_rfsf_ld_narr'] = _SIGS['oracle_d_sfrf_ld_narr']
 _SIGS['oracle_d_kin'] = [_int, _I, _I, _D, _D, _D, _D, _D, _dbl, _dbl]
 _SIGS['oracle_d_dwt_sym8'] = [_int, _I, _I, _D, _D, _D, _D]
 _SIGS['oracle_d_idwt_sym8'] = _SIGS['oracle_d_dwt_sym8']
+_SIGS['oracle_hamiltonian'] = [_I, _I, _D, _D, _D, _D, _D, _D, _D]
 
 
 def build(ref=None):
@@ -71,7 +72,7 @@ def lib():
         for name, args in _SIGS.items():
             fn = getattr(L, name)
             fn.argtypes = args
-            fn.restype = None if not name.startswith('oracle_d_') else ctypes.c_int
+            fn.restype = ctypes.c_int if name.startswith(('oracle_d_', 'oracle_hamiltonian')) else None
         _LIB = L
     return _LIB
 

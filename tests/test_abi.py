@@ -87,3 +87,22 @@ def test_declared_signatures_match_binding(pkg):
     assert len(pkg.SIGNATURES['d_s0s1_1d_sym8']) == 11      # ... a, a_y
     assert len(pkg.SIGNATURES['d_sfrf_ld_narr']) == 10      # d,n,bc,nx,ny,narr,x,y,w1,w2
     assert len(pkg.SIGNATURES['d_kin']) == 10               # d,n,bc,x,y,w1,w2,a,a_x,a_y
+
+
+def test_hamiltonian_sizes_and_validation(pkg):
+    """Host logic of the local Hamiltonian (no device call): the fine grid
+    grows by 14 and the real-space grid by 15 more along a free axis, and
+    grow/shrink boundaries are refused (the pipeline chooses them itself)."""
+    nsig, nreal, nwork = pkg.hamiltonian_sizes([5, 4, 6], [2, 0, 2])
+    assert nsig == 8 * 5 * 4 * 6
+    assert nreal == (10 + 14 + 15) * 8 * (12 + 14 + 15)
+    nf = (10 + 14) * 8 * (12 + 14)
+    assert nwork >= 2 * nf + nreal
+    assert pkg.hamiltonian_sizes([3, 3, 3], [0, 0, 0])[1] == 6 ** 3
+    for bad in ([1, 0, 0], [0, -1, 0], [0, 0, 7]):
+        with pytest.raises(pkg.LibconvError) as e:
+            pkg.hamiltonian_sizes([4, 4, 4], bad)
+        assert e.value.status == -2
+    with pytest.raises(pkg.LibconvError) as e:
+        pkg.hamiltonian_sizes([4, 0, 4], [0, 0, 0])
+    assert e.value.status == -1

@@ -328,3 +328,73 @@ def test_kinetic_ekin_restatement(O):
         assert abs(k[d] - dd.value) <= 1e-13 * abs(k[d])
     # the energies add up to x . (T x)
     assert abs(k.sum() - float(x @ r)) <= 1e-12 * abs(k.sum())
+
+
+def _rot3(f, x, dims):
+    """Apply a transposed 1D reference kernel f(x, n, ndat) along the three
+    axes in turn (each call rotates the axes, so three give the original
+    orientation); dims[i]: the input extent of axis i, f_out(i): its output."""
+    d = list(dims)
+    for _ in range(3):
+        n = d[0]
+        x = f(x, n, int(np.prod(d[1:])))
+        d = d[1:] + [x.size // int(np.prod(d[1:]))]
+    return x
+
+
+def test_hamiltonian_restatement_periodic_numpy(O, pkg):
+    """Local Hamiltonian (BigDFT/libconv.f90:248-294) with periodic axes: the
+    oracle composition against an independent numpy one built from the
+    Fortran reference kernels (synthesis, magic filter, its transpose,
+    kinetic, analysis)."""
+    n = [5, 6, 4]
+    m = [2 * v for v in n]
+    N = int(np.prod(m))
+    h = np.array([0.45, 0.4, 0.5])
+    a = -0.5 / h ** 2
+    rng = np.random.default_rng(3)
+    psig, pot = rng.standard_normal(N), rng.uniform(0.5, 1.5, N)
+    rho0 = rng.uniform(0.0, 1.0, N)
+    rho, hpsig, ek, ep = rho0.copy(), np.zeros(N), np.zeros(3), np.zeros(1)
+    assert O.call('oracle_hamiltonian', n, [0, 0, 0], a, psig, pot, rho, hpsig, ek, ep) == 0
+    def roll(x, s):
+        # the generated wavelets' real-space index k is the Fortran
+        # kernels' k+1 along every axis (LibconvBase.rb:92-96)
+        return np.roll(x.reshape(m, order='F'), s, axis=(0, 1, 2)).ravel(order='F')
+
+    fscf = roll(_rot3(lambda x, k, nd: NR.synthesis_per(x, k // 2, nd), psig, m), -1)
+    psir = _rot3(lambda x, k, nd: NR.mf_per(x, k, nd), fscf, m)
+    hpsi = _rot3(lambda x, k, nd: NR.mf_per(x, k, nd, inverse=True), pot * psir, m)
+    kin = NR.kinetic_per(fscf, m, h, 0.0)
+    want = _rot3(lambda x, k, nd: NR.analysis_per(x, k // 2, nd), roll(hpsi + kin, 1), m)
+    assert rel(hpsig, want) < 1e-13
+    assert rel(rho, rho0 + psir ** 2) < 1e-14
+    assert abs(ep[0] - float(psir @ (pot * psir))) < 1e-13 * abs(ep[0])
+    assert abs(ek.sum() - float(fscf @ kin)) < 1e-12 * abs(ek.sum())
+
+
+@pytest.mark.parametrize('bc', [[2, 2, 2], [2, 0, 2], [0, 0, 0]])
+def test_hamiltonian_restatement_symmetric(O, bc):
+    """The composed operator is self-adjoint (dwt shrink is the transpose of
+    idwt grow, the inverse magic filter shrink that of the grow one):
+    <psig|H psig> = sum ekin + epot, <phi|H psi> = <H phi|psi>, and H is
+    linear in psig."""
+    n = [5, 4, 6]
+    N = 8 * int(np.prod(n))
+    nr = int(np.prod([(2 * v + 29) if b == 2 else 2 * v for v, b in zip(n, bc)]))
+    rng = np.random.default_rng(4)
+    a = np.array([-1.3, -2.1, -0.7])
+    pot = rng.uniform(-1.0, 2.0, nr)
+    phi, psi = rng.standard_normal(N), rng.standard_normal(N)
+
+    def H(x):
+        y, ek, ep = np.zeros(N), np.zeros(3), np.zeros(1)
+        assert O.call('oracle_hamiltonian', n, bc, a, x, pot, None, y, ek, ep) == 0
+        return y, ek.sum() + ep[0]
+
+    hpsi, e = H(psi)
+    hphi, _ = H(phi)
+    assert abs(float(psi @ hpsi) - e) < 1e-13 * np.abs(psi).sum() * np.abs(hpsi).max()
+    assert abs(float(phi @ hpsi) - float(hphi @ psi)) < 1e-12 * np.abs(phi).sum() * np.abs(hpsi).max()
+    comb, _ = H(2.5 * psi - phi)
+    assert np.abs(comb - (2.5 * hpsi - hphi)).max() < 1e-12 * np.abs(comb).max()
