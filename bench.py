@@ -890,22 +890,40 @@ def run_hamiltonian(args, W):
     dx, dpot = host_x.to(dev), host_pot.to(dev)
     dh = torch.empty_like(dx)
     drho = torch.zeros(nreal, dtype=torch.float64, device=dev)
-    E = torch.zeros(B, 4, dtype=torch.float64, device=dev)
-    H = pkg.Hamiltonian(W.n, W.bc, W.a, device=dev)
+    H = pkg.Hamiltonian(W.n, W.bc, W.a, norb=B, device=dev)
     stream = torch.cuda.Stream(device=dev)
     sp = stream.cuda_stream
 
     def step():
         with torch.cuda.stream(stream):
             drho.zero_()
-        for b in range(B):
-            sl = slice(b * nsig, (b + 1) * nsig)
-            H(dx[sl], dpot, dh[sl], drho, stream=sp, energies=E[b])
+        H(dx, dpot, dh, drho, stream=sp)
 
     for _ in range(max(args.warmup, 3)):
         step()
     stream.synchronize()
     pkg.check(sp)
+
+    # the same work as one single-orbital call per orbital (no batching)
+    H1 = pkg.Hamiltonian(W.n, W.bc, W.a, device=dev)
+    E1 = torch.zeros(B, 4, dtype=torch.float64, device=dev)
+
+    def step_single():
+        with torch.cuda.stream(stream):
+            drho.zero_()
+        for b in range(B):
+            sl = slice(b * nsig, (b + 1) * nsig)
+            H1(dx[sl], dpot, dh[sl], drho, stream=sp, energies=E1[b])
+
+    step_single()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    step_single()
+    s1.record(stream)
+    s1.synchronize()
+    ms_single = s0.elapsed_time(s1)
+    del H1
+    step()
 
     def barrier():
         if world > 1:
@@ -933,30 +951,29 @@ def run_hamiltonian(args, W):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = t.item()
     value = B * world * args.steps / (ms / 1e3)
-    en = E.cpu().numpy()
+    en = H.energies.cpu().numpy()
 
-    # e2e: the host-pointer C-ABI per orbital (H2D of psig, pot and rho, D2H
-    # of hpsig, rho and the energies inside every call)
+    # e2e: the host-pointer C-ABI, one call over the B orbitals (H2D of psig,
+    # pot and rho, D2H of hpsig, rho and the energies inside every call)
     hpot = host_pot.numpy()
     hrho = torch.zeros(nreal, dtype=torch.float64, pin_memory=True).numpy()
-    pkg.hamiltonian(W.n, W.bc, W.a, hx[:nsig], hpot, hrho)
+    pkg.hamiltonian_narr(W.n, W.bc, W.a, B, hx, hpot, hrho)
     barrier()
-    e_steps = max(1, min(args.steps, 2))
+    e_steps = max(2, min(args.steps, 5))
     t0 = time.perf_counter()
     for _ in range(e_steps):
         hrho[:] = 0.0
-        for b in range(B):
-            pkg.hamiltonian(W.n, W.bc, W.a, hx[b * nsig:(b + 1) * nsig], hpot, hrho)
+        pkg.hamiltonian_narr(W.n, W.bc, W.a, B, hx, hpot, hrho)
     barrier()
     e_t = (time.perf_counter() - t0) / e_steps
     e2e = {'value': B * world / e_t, 'unit': 'orbitals/s',
-           'h2d_bytes_per_step': B * (nsig + 2 * nreal) * 8,
-           'd2h_bytes_per_step': B * (nsig + nreal + 4) * 8,
-           'note': 'libconv_hamiltonian (host pointers) once per orbital'}
+           'h2d_bytes_per_step': (B * nsig + 2 * nreal) * 8,
+           'd2h_bytes_per_step': (B * nsig + nreal + 4 * B) * 8,
+           'note': 'libconv_hamiltonian_narr (host pointers), one call over the orbitals; '
+                   'the returned hpsig array is allocated by the Python binding'}
 
     # pipeline roofline: the bytes every sweep reads and writes (the
-    # composition as separate sweeps), per orbital, against the HBM peak;
-    # the intermediates of one orbital (about 80 MB) can stay in L2
+    # composition as separate sweeps), per orbital, against the HBM peak
     n0 = [2 * v + 14 for v in W.n]
     nr = [v + 15 for v in n0]
     nf, nR = int(np.prod(n0)), int(np.prod(nr))
@@ -981,20 +998,22 @@ def run_hamiltonian(args, W):
             'compulsory_bytes_per_orbital': min_bytes,
             'compulsory_frac': min_bytes / t_orb / 1e9 / pk['hbm']}
     exact = args.mode in ('fp64', 'tc_exact')
-    launches = H.LAUNCHES['exact' if args.mode == 'tc_exact' else 'other']
+    launches = H.LAUNCHES['exact' if args.mode == 'tc_exact' else 'other']   # per call
     line = {'metric': W.metric, 'value': value, 'unit': 'orbitals/s', 'n_gpus': world,
             'steps': args.steps, 'warmup': max(args.warmup, 3), 'ms_per_step': ms / args.steps,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
             'dtype': 'f64' if exact else ('f64 in HBM, ' + args.mode[3:] + ' split on tensor cores'),
             'data': 'synthetic (seeded)',
-            'config': {'workload': f'{B} orbitals per GPU per step, 48^3 coarse points (96^3 '
+            'config': {'workload': f'{B} orbitals per GPU per step in one '
+                                   'libconv_hamiltonian_narr_dev call, 48^3 coarse points (96^3 '
                                    'coefficients), free BC: 110^3 fine and 125^3 real-space '
                                    'points; one potential, rho accumulated',
                        'mode': args.mode, 'orbitals_per_gpu': B,
+                       'single_orbital_calls_orbitals_per_s': B / (ms_single / 1e3),
                        'l2': f'inputs larger than L2 ({B * nsig * 8 / 1e6:.0f} MB of psig)',
                        'energies_orbital0': {'ekin': [float(v) for v in en[0, :3]],
                                              'epot': float(en[0, 3])}},
-            'clocks': ck, 'e2e': e2e, 'gpu_launches': args.steps * B * launches,
+            'clocks': ck, 'e2e': e2e, 'gpu_launches': args.steps * launches,
             'roofline': roof}
     if rank == 0 and world == 1 and not args.no_cpu:
         k, t, th = cpu_hamiltonian(W, base, pot, 10.0)

@@ -252,7 +252,13 @@ def _ham_lib():
         L.libconv_hamiltonian_sizes.argtypes = [_I, _I, _L, _L, _L]
         L.libconv_hamiltonian.argtypes = [_I, _I, _D, _vp, _vp, _vp, _vp, _D, _D]
         L.libconv_hamiltonian_dev.argtypes = [_I, _I, _D, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
-        for f in (L.libconv_hamiltonian_sizes, L.libconv_hamiltonian, L.libconv_hamiltonian_dev):
+        L.libconv_hamiltonian_narr_sizes.argtypes = [_I, _I, _int, _L, _L, _L]
+        L.libconv_hamiltonian_narr.argtypes = [_I, _I, _D, _int, _vp, _vp, _vp, _vp, _vp]
+        L.libconv_hamiltonian_narr_dev.argtypes = [_I, _I, _D, _int, _vp, _vp, _vp, _vp, _vp, _vp,
+                                                   _vp]
+        for f in (L.libconv_hamiltonian_sizes, L.libconv_hamiltonian, L.libconv_hamiltonian_dev,
+                  L.libconv_hamiltonian_narr_sizes, L.libconv_hamiltonian_narr,
+                  L.libconv_hamiltonian_narr_dev):
             f.restype = _int
         L._ham_bound = True
     return L
@@ -263,15 +269,34 @@ def _dbls(v):
     return ctypes.cast((ctypes.c_double * len(v))(*v), _D)
 
 
-def hamiltonian_sizes(n, bc):
-    """(nsig, nreal, nwork): elements of psig/hpsig, of the real-space grid
-    (pot, rho) and of the device workspace of the local Hamiltonian."""
+def hamiltonian_sizes(n, bc, norb=1):
+    """(nsig, nreal, nwork): elements of psig/hpsig and of the real-space grid
+    (pot, rho) per orbital, and of the device workspace of the local
+    Hamiltonian over norb orbitals."""
     L = _ham_lib()
     out = [ctypes.c_longlong(0) for _ in range(3)]
-    st = L.libconv_hamiltonian_sizes(_ints(n), _ints(bc), *[ctypes.byref(o) for o in out])
+    st = L.libconv_hamiltonian_narr_sizes(_ints(n), _ints(bc), int(norb),
+                                          *[ctypes.byref(o) for o in out])
     if st:
-        raise LibconvError(st, 'libconv_hamiltonian_sizes', last_error())
+        raise LibconvError(st, 'libconv_hamiltonian_narr_sizes', last_error())
     return tuple(o.value for o in out)
+
+
+def hamiltonian_narr(n, bc, a_kin, norb, psig, pot, rho=None):
+    """libconv_hamiltonian_narr on host arrays: norb orbitals back to back in
+    psig, one potential.  Returns (hpsig, energies[norb, 4]) with rows
+    [ekin_x, ekin_y, ekin_z, epot]; rho, when given, is updated in place."""
+    nsig, nreal, _ = hamiltonian_sizes(n, bc, norb)
+    if psig.size != norb * nsig or pot.size != nreal or (rho is not None and rho.size != nreal):
+        raise ValueError(f'psig needs {norb * nsig} and pot/rho {nreal} elements')
+    hpsig = np.zeros(norb * nsig)
+    en = np.zeros((norb, 4))
+    st = _ham_lib().libconv_hamiltonian_narr(
+        _ints(n), _ints(bc), _dbls(a_kin), int(norb), _host_ptr(psig, False),
+        _host_ptr(pot, False), _host_ptr(rho, True), _host_ptr(hpsig, True), _host_ptr(en, True))
+    if st:
+        raise LibconvError(st, 'libconv_hamiltonian_narr', last_error())
+    return hpsig, en
 
 
 def hamiltonian(n, bc, a_kin, psig, pot, rho=None):
@@ -293,16 +318,18 @@ def hamiltonian(n, bc, a_kin, psig, pot, rho=None):
 
 
 class Hamiltonian:
-    """Device form (libconv_hamiltonian_dev) with its workspace: call with
-    float64 CUDA tensors; returns the device tensor [ekin_x, ekin_y, ekin_z,
-    epot], enqueued on `stream` (no synchronisation)."""
+    """Device form (libconv_hamiltonian_narr_dev) over norb orbitals with its
+    workspace: call with float64 CUDA tensors (psig, hpsig: norb * nsig);
+    returns the device tensor of shape (norb, 4), rows [ekin_x, ekin_y,
+    ekin_z, epot], enqueued on `stream` (no synchronisation)."""
 
-    def __init__(self, n, bc, a_kin, device='cuda'):
+    def __init__(self, n, bc, a_kin, norb=1, device='cuda'):
         import torch
         self.n, self.bc, self.a_kin = list(n), list(bc), [float(v) for v in a_kin]
-        self.nsig, self.nreal, nwork = hamiltonian_sizes(n, bc)
+        self.norb = int(norb)
+        self.nsig, self.nreal, nwork = hamiltonian_sizes(n, bc, self.norb)
         self.work = torch.empty(nwork, dtype=torch.float64, device=device)
-        self.energies = torch.zeros(4, dtype=torch.float64, device=device)
+        self.energies = torch.zeros(self.norb, 4, dtype=torch.float64, device=device)
 
     # kernel launches of one call: 15 sweeps (x2 in the exact tensor-core mode,
     # whose sweeps each follow a line-exponent pass), the potential kernel and
@@ -310,21 +337,22 @@ class Hamiltonian:
     LAUNCHES = {'exact': 35, 'other': 20}
 
     def __call__(self, psig, pot, hpsig, rho=None, stream=None, energies=None):
-        """energies: optional device tensor of 4 doubles to receive
-        [ekin_x, ekin_y, ekin_z, epot] instead of the object's own buffer."""
+        """energies: optional device tensor of norb * 4 doubles to receive the
+        energies instead of the object's own buffer."""
         en = self.energies if energies is None else energies
-        if en.numel() != 4:
-            raise ValueError('energies needs 4 elements')
-        if psig.numel() != self.nsig or hpsig.numel() != self.nsig or pot.numel() != self.nreal:
-            raise ValueError(f'psig/hpsig need {self.nsig} and pot {self.nreal} elements')
+        ns = self.norb * self.nsig
+        if en.numel() != 4 * self.norb:
+            raise ValueError(f'energies needs {4 * self.norb} elements')
+        if psig.numel() != ns or hpsig.numel() != ns or pot.numel() != self.nreal:
+            raise ValueError(f'psig/hpsig need {ns} and pot {self.nreal} elements')
         if rho is not None and rho.numel() != self.nreal:
             raise ValueError(f'rho needs {self.nreal} elements')
-        st = _ham_lib().libconv_hamiltonian_dev(
-            _ints(self.n), _ints(self.bc), _dbls(self.a_kin), _dev_ptr(psig), _dev_ptr(pot),
-            _dev_ptr(rho), _dev_ptr(hpsig), _dev_ptr(en), _dev_ptr(self.work),
+        st = _ham_lib().libconv_hamiltonian_narr_dev(
+            _ints(self.n), _ints(self.bc), _dbls(self.a_kin), self.norb, _dev_ptr(psig),
+            _dev_ptr(pot), _dev_ptr(rho), _dev_ptr(hpsig), _dev_ptr(en), _dev_ptr(self.work),
             _stream_ptr(stream))
         if st:
-            raise LibconvError(st, 'libconv_hamiltonian_dev', last_error())
+            raise LibconvError(st, 'libconv_hamiltonian_narr_dev', last_error())
         return en
 
 

@@ -14,6 +14,7 @@ struct PlanStep {
     Sweep S;
     int src, dst, src2;   // buffer ids (src2 = -1 if no x2)
     int dot_slot = 0;     // entry of the dot output this step's dot product goes to
+    int dot_stride = 0;   // > 0: one dot per array, array j at dot_slot + j * dot_stride
 };
 
 struct Plan {

@@ -49,11 +49,17 @@ cudaError_t launch_sweep_fp64_batch(int kind, int ntaps, int qc, const Sweep *de
 // Deterministic sum of `count` partials into *out (device), on `st`.
 cudaError_t launch_dot_reduce(const double *part, long long count, double *out, int accumulate,
                               cudaStream_t st);
-// Potential step of the local Hamiltonian on `count` real-space points:
-// rho += psir^2 (rho may be null), *epot = sum pot psir^2, psir = pot psir.
-// part holds potential_blocks(count, sms) partial sums.
-int potential_blocks(long long count, int sms);
+// Segmented form: out[j * out_stride] = sum of part[j*seg_len .. (j+1)*seg_len)
+// for j < nseg (fixed order), on `st`.
+cudaError_t launch_dot_reduce_seg(const double *part, long long seg_len, int nseg, double *out,
+                                  long long out_stride, cudaStream_t st);
+// Potential step of the local Hamiltonian over norb orbitals of `count`
+// real-space points each (psir back to back): rho += sum_j psir_j^2 (rho may
+// be null), epot[j * epot_stride] = sum pot psir_j^2, psir_j = pot psir_j.
+// part holds potential_blocks(count) * norb partial sums.
+long long potential_blocks(long long count);
 cudaError_t launch_potential(double *psir, const double *pot, double *rho, long long count,
-                             double *part, int nblocks, double *epot, cudaStream_t st);
+                             int norb, double *part, double *epot, long long epot_stride,
+                             cudaStream_t st);
 
 }  // namespace lcg

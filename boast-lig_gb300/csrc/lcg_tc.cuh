@@ -27,6 +27,9 @@ struct TcFilter {
 void tc_filter_digits(const double *taps, int ntaps, double a, TcFilter &F);
 void tc_filter_split(const double *taps, int ntaps, double a, int sch, TcFilter &F);
 bool sweep_tc_supported(const Sweep &S);
+// CTAs of the (non-batched) tensor-core sweep of S.  Its dot partials: 8
+// per CTA per array, array-major (sweep_tc_blocks(S) * 8 per array); the
+// slots of an array a CTA has no tile of are not written.
 long long sweep_tc_blocks(const Sweep &S);
 // status (device int) is set non-zero if a tensor-core wait timed out.
 // lineE (exact scheme, or null): device scratch of sweep_tc_lines(S) ints; the

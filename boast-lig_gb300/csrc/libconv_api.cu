@@ -375,12 +375,22 @@ int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, DevBuf &line
         if (!S.x || !S.y || (ps.src2 >= 0 && !S.x2))
             return fail(LIBCONV_EARG, "null device buffer in plan");
         const bool tc = t_mode != LIBCONV_MODE_FP64 && sweep_tc_supported(S);
-        long long nb = 0;
+        long long nb = 0, seg = 0;   // dot partials: total, and per array (array-major)
         if (S.has_dot) {
-            nb = tc ? sweep_tc_blocks(S) : sweep_fp64_blocks(S);
+            if (tc) {
+                seg = sweep_tc_blocks(S) * 8;
+                nb = seg * S.narr;
+            } else {
+                nb = sweep_fp64_blocks(S);
+                seg = nb / S.narr;
+            }
             int rc = ensure(scratch, (size_t)nb * sizeof(double));
             if (rc) return rc;
             S.dot_part = (double *)scratch.p;
+            if (tc && S.narr > 1) {   // slots of arrays a CTA has no tile of stay 0
+                cudaError_t e = cudaMemsetAsync(S.dot_part, 0, (size_t)nb * sizeof(double), st);
+                if (e != cudaSuccess) return cuda_fail(e, "clear dot partials");
+            }
         }
         cudaError_t e;
         if (tc) {
@@ -404,7 +414,10 @@ int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, DevBuf &line
         }
         if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
         if (S.has_dot) {
-            e = launch_dot_reduce(S.dot_part, nb, dot_dev + ps.dot_slot, 0, st);
+            e = ps.dot_stride > 0
+                    ? launch_dot_reduce_seg(S.dot_part, seg, S.narr, dot_dev + ps.dot_slot,
+                                            ps.dot_stride, st)
+                    : launch_dot_reduce(S.dot_part, nb, dot_dev + ps.dot_slot, 0, st);
             if (e != cudaSuccess) return cuda_fail(e, "dot reduction launch");
         }
     }
@@ -478,19 +491,23 @@ int exec_host(const Plan &P, const double *x, double *y, double *dot_host) {
 // idwt (grow) -> MagicFilter (grow) -> density and potential -> inverse
 // MagicFilter (shrink) -> kinetic with dot, accumulated (no-grow, a_y = 1)
 // -> dwt (shrink).  Free axes take that grow/shrink chain; periodic axes are
-// periodic in every step.
+// periodic in every step.  norb orbitals lie back to back and every step is
+// one launch over all of them (narr = norb), so a sweep covers norb grids'
+// worth of tiles; the energies are kept per orbital (segmented dots).
 struct Ham {
     Plan idwt, mf, imf, kin, dwt;
+    int norb = 1;
     int n0[3], nr[3];      // fine-grid extents of psi_fscf / hpsi and of psir
-    size_t nsig = 0;       // elements of psig and hpsig
-    size_t nfscf = 0;      // elements of psi_fscf and hpsi
-    size_t nreal = 0;      // elements of psir, pot and rho
-    size_t nw = 0;         // elements of each ping-pong workspace (w1, w2)
-    size_t nwork() const { return 2 * nfscf + nreal + 2 * nw; }
+    size_t nsig = 0;       // elements of psig and hpsig, per orbital
+    size_t nfscf = 0;      // elements of psi_fscf and hpsi, per orbital
+    size_t nreal = 0;      // elements of psir, pot and rho, per orbital
+    size_t nw = 0;         // elements of each ping-pong workspace (w1, w2), all orbitals
+    size_t nwork() const { return (size_t)norb * (2 * nfscf + nreal) + 2 * nw; }
 };
 
-int plan_ham(const int *n, const int *bc, const double *a_kin, Ham &H) {
+int plan_ham(const int *n, const int *bc, const double *a_kin, int norb, Ham &H) {
     if (!n || !bc || !a_kin) return fail(LIBCONV_EARG, "n/bc/a_kin must not be null");
+    if (norb < 1 || norb > 65535) return fail(LIBCONV_EARG, "norb=%d out of [1,65535]", norb);
     int bw[3], bi[3], bk[3];
     for (int i = 0; i < 3; ++i) {
         if (n[i] < 1) return fail(LIBCONV_EARG, "n[%d]=%d", i, n[i]);
@@ -505,36 +522,40 @@ int plan_ham(const int *n, const int *bc, const double *a_kin, Ham &H) {
         H.n0[i] = 2 * need_out(OP_IWT, bw[i], n[i]);
         H.nr[i] = need_out(OP_MD, bw[i], H.n0[i]);
     }
+    H.norb = norb;
     int rc;
-    if ((rc = plan_md_t(OP_IWT, 3, n, bw, nullptr, nullptr, 1, H.idwt))) return rc;
-    if ((rc = plan_md_t(OP_MD, 3, H.n0, bw, nullptr, nullptr, 1, H.mf))) return rc;
-    if ((rc = plan_md_t(OP_IMD, 3, H.n0, bi, nullptr, nullptr, 1, H.imf))) return rc;
-    if ((rc = plan_kin(3, H.n0, bk, a_kin, 0.0, 1.0, H.kin, 1, nullptr, true))) return rc;
-    if ((rc = plan_md_t(OP_DWT, 3, n, bi, nullptr, nullptr, 1, H.dwt))) return rc;
+    if ((rc = plan_md_t(OP_IWT, 3, n, bw, nullptr, nullptr, norb, H.idwt))) return rc;
+    if ((rc = plan_md_t(OP_MD, 3, H.n0, bw, nullptr, nullptr, norb, H.mf))) return rc;
+    if ((rc = plan_md_t(OP_IMD, 3, H.n0, bi, nullptr, nullptr, norb, H.imf))) return rc;
+    if ((rc = plan_kin(3, H.n0, bk, a_kin, 0.0, 1.0, H.kin, norb, nullptr, true))) return rc;
+    if ((rc = plan_md_t(OP_DWT, 3, n, bi, nullptr, nullptr, norb, H.dwt))) return rc;
+    for (PlanStep &ps : H.kin.steps) ps.dot_stride = 4;   // energies[j][i], j = orbital
     H.nsig = 8ull * n[0] * n[1] * n[2];
     H.nfscf = (size_t)H.n0[0] * H.n0[1] * H.n0[2];
     H.nreal = (size_t)H.nr[0] * H.nr[1] * H.nr[2];
+    if ((double)H.nreal * norb > 9.0e15) return fail(LIBCONV_EARG, "grid too large");
     for (const Plan *P : {&H.idwt, &H.mf, &H.imf, &H.kin, &H.dwt})
         for (int b : {B_W1, B_W2}) if (P->elems[b] > H.nw) H.nw = P->elems[b];
     return LIBCONV_OK;
 }
 
 // Enqueue the pipeline on `st`.  work: H.nwork() doubles; energies: 4
-// doubles (ekin of the three directions, then epot), device pointers.
+// doubles per orbital (ekin of the three directions, then epot), device.
 int run_ham(const Ham &H, const double *psig, const double *pot, double *rho, double *hpsig,
             double *work, double *energies, DevState &s, cudaStream_t st) {
-    double *fscf = work, *hpsi = fscf + H.nfscf, *psir = hpsi + H.nfscf;
-    double *w1 = psir + H.nreal, *w2 = w1 + H.nw;
+    const size_t no = (size_t)H.norb;
+    double *fscf = work, *hpsi = fscf + no * H.nfscf, *psir = hpsi + no * H.nfscf;
+    double *w1 = psir + no * H.nreal, *w2 = w1 + H.nw;
     int *status = (int *)s.status.p;
     double *b_idwt[4] = {const_cast<double *>(psig), fscf, w1, w2};
     int rc = run_plan(H.idwt, b_idwt, s.scratch, s.lineexp, nullptr, status, st);
     if (rc) return rc;
     double *b_mf[4] = {fscf, psir, w1, w2};
     if ((rc = run_plan(H.mf, b_mf, s.scratch, s.lineexp, nullptr, status, st))) return rc;
-    const int nb = potential_blocks((long long)H.nreal, tck::sm_count());
-    if ((rc = ensure(s.potpart, (size_t)nb * sizeof(double)))) return rc;
-    cudaError_t e = launch_potential(psir, pot, rho, (long long)H.nreal, (double *)s.potpart.p, nb,
-                                     energies + 3, st);
+    const long long nb = potential_blocks((long long)H.nreal);
+    if ((rc = ensure(s.potpart, (size_t)nb * no * sizeof(double)))) return rc;
+    cudaError_t e = launch_potential(psir, pot, rho, (long long)H.nreal, H.norb,
+                                     (double *)s.potpart.p, energies + 3, 4, st);
     if (e != cudaSuccess) return cuda_fail(e, "potential launch");
     double *b_imf[4] = {psir, hpsi, w1, w2};
     if ((rc = run_plan(H.imf, b_imf, s.scratch, s.lineexp, nullptr, status, st))) return rc;
@@ -542,6 +563,40 @@ int run_ham(const Ham &H, const double *psig, const double *pot, double *rho, do
     if ((rc = run_plan(H.kin, b_kin, s.scratch, s.lineexp, energies, status, st))) return rc;
     double *b_dwt[4] = {hpsi, hpsig, w1, w2};
     return run_plan(H.dwt, b_dwt, s.scratch, s.lineexp, nullptr, status, st);
+}
+
+// Host-pointer form: stage in the library's device buffer, run, copy back.
+// energies: 4 doubles per orbital (host).
+int ham_host(const Ham &H, const double *psig, const double *pot, double *rho, double *hpsig,
+             double *energies) {
+    if (!psig || !pot || !hpsig || !energies)
+        return fail(LIBCONV_EARG, "psig/pot/hpsig/energies must not be null");
+    std::lock_guard<std::mutex> lk(g_mu);
+    int rc;
+    DevState *s = dev_state(rc);
+    if (!s) return rc;
+    const size_t no = (size_t)H.norb, ns = no * H.nsig;
+    const size_t nd = 2 * ns + (rho ? 2 : 1) * H.nreal + H.nwork() + 4 * no;
+    if ((rc = ensure(s->hbuf, nd * sizeof(double)))) return rc;
+    double *d_psig = (double *)s->hbuf.p, *d_hpsig = d_psig + ns, *d_pot = d_hpsig + ns;
+    double *d_rho = rho ? d_pot + H.nreal : nullptr;
+    double *d_work = d_pot + (rho ? 2 : 1) * H.nreal, *d_en = d_work + H.nwork();
+    cudaStream_t st = s->stream;
+    cudaError_t e = cudaMemcpyAsync(d_psig, psig, ns * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_pot, pot, H.nreal * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && rho)
+        e = cudaMemcpyAsync(d_rho, rho, H.nreal * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "copy inputs to device");
+    if ((rc = run_ham(H, d_psig, d_pot, d_rho, d_hpsig, d_work, d_en, *s, st))) return rc;
+    e = cudaMemcpyAsync(hpsig, d_hpsig, ns * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && rho)
+        e = cudaMemcpyAsync(rho, d_rho, H.nreal * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(energies, d_en, 4 * no * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "copy outputs to host");
+    return read_status(*s);
 }
 
 // ---- cost model (GenericConvolution2.rb:1269-1276, 1525-1558, 1850-1932) ----
@@ -841,9 +896,14 @@ int d_kin_narr_dev(int d, const int *n, const int *bc, int narr, const double *x
 
 int libconv_hamiltonian_sizes(const int *n, const int *bc, long long *nsig, long long *nreal,
                               long long *nwork) {
+    return libconv_hamiltonian_narr_sizes(n, bc, 1, nsig, nreal, nwork);
+}
+
+int libconv_hamiltonian_narr_sizes(const int *n, const int *bc, int norb, long long *nsig,
+                                   long long *nreal, long long *nwork) {
     Ham H;
     const double a1[3] = {1.0, 1.0, 1.0};
-    int rc = plan_ham(n, bc, a1, H);
+    int rc = plan_ham(n, bc, a1, norb, H);
     if (rc) return rc;
     if (nsig) *nsig = (long long)H.nsig;
     if (nreal) *nreal = (long long)H.nreal;
@@ -853,35 +913,12 @@ int libconv_hamiltonian_sizes(const int *n, const int *bc, long long *nsig, long
 
 int libconv_hamiltonian(const int *n, const int *bc, const double *a_kin, const double *psig,
                         const double *pot, double *rho, double *hpsig, double *ekin, double *epot) {
-    if (!psig || !pot || !hpsig || !ekin || !epot)
-        return fail(LIBCONV_EARG, "psig/pot/hpsig/ekin/epot must not be null");
+    if (!ekin || !epot) return fail(LIBCONV_EARG, "ekin/epot must not be null");
     Ham H;
-    int rc = plan_ham(n, bc, a_kin, H);
+    int rc = plan_ham(n, bc, a_kin, 1, H);
     if (rc) return rc;
-    std::lock_guard<std::mutex> lk(g_mu);
-    DevState *s = dev_state(rc);
-    if (!s) return rc;
-    const size_t nd = 2 * H.nsig + (rho ? 2 : 1) * H.nreal + H.nwork() + 4;
-    if ((rc = ensure(s->hbuf, nd * sizeof(double)))) return rc;
-    double *d_psig = (double *)s->hbuf.p, *d_hpsig = d_psig + H.nsig, *d_pot = d_hpsig + H.nsig;
-    double *d_rho = rho ? d_pot + H.nreal : nullptr;
-    double *d_work = d_pot + (rho ? 2 : 1) * H.nreal, *d_en = d_work + H.nwork();
-    cudaStream_t st = s->stream;
-    cudaError_t e = cudaMemcpyAsync(d_psig, psig, H.nsig * sizeof(double), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_pot, pot, H.nreal * sizeof(double), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && rho)
-        e = cudaMemcpyAsync(d_rho, rho, H.nreal * sizeof(double), cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return cuda_fail(e, "copy inputs to device");
-    if ((rc = run_ham(H, d_psig, d_pot, d_rho, d_hpsig, d_work, d_en, *s, st))) return rc;
     double en[4];
-    e = cudaMemcpyAsync(hpsig, d_hpsig, H.nsig * sizeof(double), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess && rho)
-        e = cudaMemcpyAsync(rho, d_rho, H.nreal * sizeof(double), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(en, d_en, sizeof en, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return cuda_fail(e, "copy outputs to host");
-    if ((rc = read_status(*s))) return rc;
+    if ((rc = ham_host(H, psig, pot, rho, hpsig, en))) return rc;
     for (int i = 0; i < 3; ++i) ekin[i] = en[i];
     *epot = en[3];
     return LIBCONV_OK;
@@ -890,10 +927,25 @@ int libconv_hamiltonian(const int *n, const int *bc, const double *a_kin, const 
 int libconv_hamiltonian_dev(const int *n, const int *bc, const double *a_kin, const double *psig,
                             const double *pot, double *rho, double *hpsig, double *energies,
                             double *work, void *stream) {
+    return libconv_hamiltonian_narr_dev(n, bc, a_kin, 1, psig, pot, rho, hpsig, energies, work,
+                                        stream);
+}
+
+int libconv_hamiltonian_narr(const int *n, const int *bc, const double *a_kin, int norb,
+                             const double *psig, const double *pot, double *rho, double *hpsig,
+                             double *energies) {
+    Ham H;
+    int rc = plan_ham(n, bc, a_kin, norb, H);
+    return rc ? rc : ham_host(H, psig, pot, rho, hpsig, energies);
+}
+
+int libconv_hamiltonian_narr_dev(const int *n, const int *bc, const double *a_kin, int norb,
+                                 const double *psig, const double *pot, double *rho,
+                                 double *hpsig, double *energies, double *work, void *stream) {
     if (!psig || !pot || !hpsig || !energies || !work)
         return fail(LIBCONV_EARG, "psig/pot/hpsig/energies/work must not be null");
     Ham H;
-    int rc = plan_ham(n, bc, a_kin, H);
+    int rc = plan_ham(n, bc, a_kin, norb, H);
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(g_mu);
     DevState *s = dev_state(rc);

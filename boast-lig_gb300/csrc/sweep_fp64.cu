@@ -212,9 +212,13 @@ sweep_fp64_batch_kernel(const Sweep *__restrict__ descs, const long long *__rest
     }
 }
 
+// Block b sums part[b*count .. (b+1)*count) in a fixed order into
+// out[b*out_stride] (one block per segment: per-array dot products).
 __global__ void dot_reduce_kernel(const double *__restrict__ part, long long count, double *out,
-                                  int accumulate) {
+                                  long long out_stride, int accumulate) {
     __shared__ double red[256];
+    part += (long long)blockIdx.x * count;
+    out += (long long)blockIdx.x * out_stride;
     double s = 0.0;
     for (long long i = threadIdx.x; i < count; i += blockDim.x) s += part[i];
     red[threadIdx.x] = s;
@@ -313,7 +317,14 @@ cudaError_t launch_sweep_fp64_batch(int kind, int ntaps, int qc, const Sweep *de
 
 cudaError_t launch_dot_reduce(const double *part, long long count, double *out, int accumulate,
                               cudaStream_t st) {
-    dot_reduce_kernel<<<1, 256, 0, st>>>(part, count, out, accumulate);
+    dot_reduce_kernel<<<1, 256, 0, st>>>(part, count, out, 0, accumulate);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dot_reduce_seg(const double *part, long long seg_len, int nseg, double *out,
+                                  long long out_stride, cudaStream_t st) {
+    if (nseg < 1 || nseg > 65535) return cudaErrorInvalidValue;
+    dot_reduce_kernel<<<nseg, 256, 0, st>>>(part, seg_len, out, out_stride, 0);
     return cudaGetLastError();
 }
 

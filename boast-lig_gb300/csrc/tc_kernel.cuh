@@ -375,7 +375,6 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
     uint8_t *aux = B + G::B_BYTES;
     uint64_t *bars = (uint64_t *)aux;                 // 8 barriers
     uint32_t *tslot = (uint32_t *)(aux + 64);
-    double *red = (double *)(aux + 128);              // 8 doubles
     int *rowE = (int *)(aux + 1024);                  // producers -> MMA issuer
     int *rowE_epi = rowE + kM;                        // MMA issuer -> epilogue, by tile parity
     const uint32_t bA_full = saddr(&bars[0]), bA_empty = saddr(&bars[1]);
@@ -406,7 +405,6 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
         }
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    if (tid < 8) red[tid] = 0.0;
     // Toeplitz filter tiles B_t[n][kk], K-major core matrices
     for (int idx = tid; idx < G::ND * 16 * G::KB; idx += kThreads) {
         const int t = idx / (16 * G::KB), rem = idx % (16 * G::KB);
@@ -615,7 +613,16 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
         const int ew = warp - kProducers / 32;
         const int lq = ew & 3, hf = ew >> 2;
         const int row = lq * 32 + lane;
+        // dot products per array: each epilogue warp owns the slot
+        // dot_part[(arr * gridDim.x + blockIdx.x) * 8 + ew] of every array it
+        // visits (tiles are array-major, so a CTA meets the arrays in order)
         double dot = 0.0;
+        int dot_arr = -1;
+        auto flush_dot = [&]() {
+            for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+            if (lane == 0) S0.dot_part[((long long)dot_arr * gridDim.x + blockIdx.x) * 8 + ew] = dot;
+            dot = 0.0;
+        };
         uint32_t it = 0;
         for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
             if (!bar_wait(bX_full[hf], it & 1)) { alive = false; break; }
@@ -630,6 +637,10 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             const int ch = (int)(loc.t % nch);
             const long long lb = (loc.t / nch) % nlb;
             const int arr = (int)(loc.t / (nch * nlb));
+            if (!BATCH && S0.has_dot && arr != dot_arr) {
+                if (dot_arr >= 0) flush_dot();
+                dot_arr = arr;
+            }
             const int qc0 = S.qlo + ch * G::QP;
             const long long out_pext = (long long)S.out_ext * NCH;
             const long long g = lb * kM + row;
@@ -712,10 +723,11 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                     }
                     double *const yp = ystep + yps * (n / NCH) + ycs * c;
                     if (KIND == KCONV) {
-                        if ((S.has_dot || S.has_ax) && (!grow || (q >= 0 && q < S.n))) {
+                        const bool want_dot = !BATCH && S.has_dot;   // batched sweeps have no dot
+                        if ((want_dot || S.has_ax) && (!grow || (q >= 0 && q < S.n))) {
                             const int ps = S.bc == BC_PERIODIC ? imod(q, S.n) : q - S.in_lo;
                             const double xq = xrow[(long long)S.nL * ps];
-                            if (S.has_dot) dot = fma(xq, out, dot);
+                            if (want_dot) dot = fma(xq, out, dot);
                             if (S.has_ax) out = fma(xq, S.a_x, out);
                         }
                         if (x2) out += add[n];
@@ -726,10 +738,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                 }
             }
         }
-        if (S0.has_dot) {
-            for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
-            if (lane == 0) red[ew] = dot;
-        }
+        if (!BATCH && S0.has_dot && dot_arr >= 0) flush_dot();
     }
 
     if (!alive) atomicExch(status, 1);
@@ -739,11 +748,6 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
                      "r"(G::TMEM_COLS)
                      : "memory");
-    if (S0.has_dot && tid == 0) {
-        double sdot = 0.0;
-        for (int i = 0; i < 8; ++i) sdot += red[i];
-        S0.dot_part[blockIdx.x] = sdot;
-    }
 }
 
 template <int KIND, int NT, int SCH, bool BATCH>

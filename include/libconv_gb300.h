@@ -268,6 +268,22 @@ int libconv_hamiltonian(const int *n, const int *bc, const double *a_kin, const 
 int libconv_hamiltonian_dev(const int *n, const int *bc, const double *a_kin, const double *psig,
                             const double *pot, double *rho, double *hpsig, double *energies,
                             double *work, void *stream);
+/* norb orbitals at once (psig and hpsig: norb arrays of nsig back to back),
+ * sharing one potential; every step is one launch over all orbitals.  rho
+ * (when not NULL) accumulates psir_j^2 for j = 0..norb-1 in order, giving
+ * the same numbers as norb single-orbital calls.  energies: norb x 4
+ * doubles, [ekin_x, ekin_y, ekin_z, epot] of each orbital (host pointer for
+ * libconv_hamiltonian_narr, device pointer for the _dev form).  nwork of
+ * libconv_hamiltonian_narr_sizes grows with norb (about 10 nsig per
+ * orbital). */
+int libconv_hamiltonian_narr_sizes(const int *n, const int *bc, int norb, long long *nsig,
+                                   long long *nreal, long long *nwork);
+int libconv_hamiltonian_narr(const int *n, const int *bc, const double *a_kin, int norb,
+                             const double *psig, const double *pot, double *rho, double *hpsig,
+                             double *energies);
+int libconv_hamiltonian_narr_dev(const int *n, const int *bc, const double *a_kin, int norb,
+                                 const double *psig, const double *pot, double *rho,
+                                 double *hpsig, double *energies, double *work, void *stream);
 
 /* ---------------------------------------------------------------------
  * Cost model (ConvolutionOperator1d#cost / GenericConvolutionOperator#cost,

@@ -92,9 +92,63 @@ def test_hamiltonian_device_entry(pkg, O):
     ho, eo, po = oracle_ham(O, n, bc, a, psig, pot, ro)
     assert rel(dh.cpu().numpy(), ho) <= TOL
     assert rel(drho.cpu().numpy(), ro) <= TOL
-    e = en.cpu().numpy()
+    e = en.cpu().numpy().ravel()
     assert np.abs(e[:3] - eo).max() <= ETOL * np.abs(eo).max()
     assert abs(e[3] - po) <= ETOL * np.abs(pot).max() * float(np.abs(ro - rho0).sum())
+
+
+@pytest.mark.parametrize('n,bc,norb', [
+    ([6, 5, 7], [2, 2, 2], 3),    # few tiles per orbital: CTAs skip orbitals
+    ([8, 8, 6], [0, 0, 0], 4),
+    ([7, 4, 9], [2, 0, 2], 2),
+])
+def test_hamiltonian_narr_matches_single_orbitals(pkg, O, n, bc, norb):
+    """norb orbitals in one call: hpsig of every orbital bit-identical to the
+    single-orbital call (same sweeps, only batched), rho bit-identical to
+    the single-orbital calls made in order, per-orbital energies as the
+    oracle's."""
+    a = [-1.7, -2.2, -0.9]
+    nsig, nreal, _ = pkg.hamiltonian_sizes(n, bc)
+    rng = np.random.default_rng(21)
+    psig = rng.standard_normal(norb * nsig) * np.repeat(1.0 + np.arange(norb), nsig)
+    pot = rng.uniform(-1.0, 2.0, nreal)
+    rho0 = rng.uniform(0.0, 1.0, nreal)
+    rb = rho0.copy()
+    hb, eb = pkg.hamiltonian_narr(n, bc, a, norb, psig, pot, rb)
+    assert eb.shape == (norb, 4)
+    rs, ro = rho0.copy(), rho0.copy()
+    for j in range(norb):
+        sl = slice(j * nsig, (j + 1) * nsig)
+        hs, es, ps = pkg.hamiltonian(n, bc, a, psig[sl], pot, rs)
+        assert np.array_equal(hb[sl], hs), j
+        ho, eo, po = oracle_ham(O, n, bc, a, psig[sl].copy(), pot, ro)
+        assert rel(hb[sl], ho) <= TOL
+        assert np.abs(eb[j, :3] - eo).max() <= ETOL * np.abs(eo).max(), (j, eb[j], eo)
+        assert abs(eb[j, 3] - po) <= ETOL * 2 * float(psig[sl] @ psig[sl]) * np.abs(pot).max()
+    assert np.array_equal(rb, rs)
+    assert rel(rb, ro) <= TOL
+
+
+def test_hamiltonian_narr_device_entry(pkg, O):
+    import torch
+    n, bc, norb = [5, 6, 5], [2, 2, 2], 5
+    a = [-1.0, -1.2, -1.4]
+    nsig, nreal, _ = pkg.hamiltonian_sizes(n, bc)
+    rng = np.random.default_rng(22)
+    psig, pot = rng.standard_normal(norb * nsig), rng.uniform(0.1, 1.0, nreal)
+    H = pkg.Hamiltonian(n, bc, a, norb=norb)
+    dpsig, dpot = torch.from_numpy(psig).cuda(), torch.from_numpy(pot).cuda()
+    dh = torch.zeros_like(dpsig)
+    en = H(dpsig, dpot, dh)
+    torch.cuda.synchronize()
+    pkg.check()
+    e = en.cpu().numpy()
+    for j in range(norb):
+        sl = slice(j * nsig, (j + 1) * nsig)
+        ho, eo, po = oracle_ham(O, n, bc, a, psig[sl].copy(), pot, None)
+        assert rel(dh[sl].cpu().numpy(), ho) <= TOL
+        assert np.abs(e[j, :3] - eo).max() <= ETOL * np.abs(eo).max()
+        assert abs(e[j, 3] - po) <= ETOL * abs(po)
 
 
 def test_hamiltonian_repeated_calls_identical(pkg):
