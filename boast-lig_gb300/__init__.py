@@ -23,6 +23,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, 'libconv_gb300.so')
 HEADER = os.path.join(HERE, '..', 'include', 'libconv_gb300.h')
+FORTRAN_HEADER = os.path.join(HERE, '..', 'include', 'libconv_fortran.h')
 
 BC_SHRINK, BC_PERIODIC, BC_GROW, BC_FREE = -1, 0, 1, 2
 MODE_FP64 = 0
@@ -99,8 +100,9 @@ def lib():
 
 
 def declared_symbols():
-    """Every function name declared in include/libconv_gb300.h."""
-    text = open(HEADER).read()
+    """Every function name declared in include/libconv_gb300.h and
+    include/libconv_fortran.h."""
+    text = open(HEADER).read() + open(FORTRAN_HEADER).read()
     text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
     return sorted(set(re.findall(r'\b(?:int|const char \*|void)\s*\**\s*(\w+)\s*\(', text)))
 
@@ -354,6 +356,76 @@ class Hamiltonian:
         if st:
             raise LibconvError(st, 'libconv_hamiltonian_narr_dev', last_error())
         return en
+
+
+# ---- Fortran-facing libconv procedures (include/libconv_fortran.h) ----------------
+class Fortran:
+    """Calls the Fortran-facing procedures the way gfortran does: every
+    argument by reference (ints, doubles, int arrays, float64 arrays), and
+    CHARACTER arguments with their hidden length at the end.  Raises on a
+    non-zero libconv_status."""
+
+    def __init__(self):
+        self.L = lib()
+
+    @staticmethod
+    def _ref(v):
+        if isinstance(v, np.ndarray):
+            return ctypes.c_void_p(v.ctypes.data)
+        if isinstance(v, (list, tuple)):
+            return ctypes.cast((ctypes.c_int * len(v))(*[int(t) for t in v]), ctypes.c_void_p)
+        if isinstance(v, float):
+            return ctypes.cast(ctypes.pointer(ctypes.c_double(v)), ctypes.c_void_p)
+        if isinstance(v, int):
+            return ctypes.cast(ctypes.pointer(ctypes.c_int(v)), ctypes.c_void_p)
+        if v is None:
+            return None
+        raise TypeError(f'unsupported Fortran argument {type(v)}')
+
+    def status(self):
+        st = ctypes.c_int(0)
+        self.L.libconv_status_(ctypes.byref(st))
+        return st.value
+
+    def call(self, name, *args, check=True):
+        fn = getattr(self.L, name + '_')
+        fn.restype = None
+        fn(*[self._ref(a) for a in args])
+        st = self.status()
+        if check and st:
+            raise LibconvError(st, name, last_error())
+        return st
+
+    def filter_id(self, name):
+        fid = ctypes.c_int(0)
+        b = name.encode()
+        self.L.get_filter_id_(ctypes.c_char_p(b), ctypes.byref(fid), ctypes.c_size_t(len(b)))
+        return fid.value
+
+    def bc_id(self, name):
+        bid = ctypes.c_int(0)
+        b = name.encode()
+        self.L.get_bc_id_(ctypes.c_char_p(b), ctypes.byref(bid), ctypes.c_size_t(len(b)))
+        return bid.value
+
+    def filter_name(self, fid, length=16):
+        buf = ctypes.create_string_buffer(length)
+        self.L.get_filter_name_(ctypes.byref(ctypes.c_int(fid)), buf, ctypes.c_size_t(length))
+        return buf.raw.decode().rstrip()
+
+    def bc_name(self, bid, length=4):
+        buf = ctypes.create_string_buffer(length)
+        self.L.get_bc_name_(ctypes.byref(ctypes.c_int(bid)), buf, ctypes.c_size_t(length))
+        return buf.raw.decode().rstrip()
+
+    def sizes(self, name, d, n, fil, bc, work=False):
+        out = (ctypes.c_int * (1 if work else d))()
+        getattr(self.L, name + '_')(self._ref(d), self._ref(list(n)), self._ref(fil),
+                                    self._ref(list(bc)), out)
+        st = self.status()
+        if st:
+            raise LibconvError(st, name, last_error())
+        return out[0] if work else list(out)
 
 
 # ---- batched operators over many uneven grids ------------------------------------

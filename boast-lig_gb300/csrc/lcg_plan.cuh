@@ -38,6 +38,19 @@ const double *filter_table();
 int current_mode();
 // Device status word of the current device (bounded tensor-core waits).
 int *device_status(int &rc);
+// Operators of the Fortran-facing layer.
+enum OpId { OPID_MD, OPID_IMD, OPID_D1, OPID_D2, OPID_DWT, OPID_IWT, OPID_RTOS1, OPID_S1TOR };
+// Multi-D product y = a F x + a_y y (a_x: d = 1 convolutions only), host pointers.
+int md_generic(int op_id, int d, const int *n, const int *bc, const int *nx, const int *ny,
+               int narr, double a, double a_x, double a_y, const double *x, double *y);
+// Sum of 1D convolutions y = sum_i a[i] F_i x + a_x x + a_y y, dot[i] = x . (a[i] F_i x)
+// when dot is not null; host pointers.
+int sum1d_generic(int op_id, int d, const int *n, const int *bc, const int *nx, const int *ny,
+                  int narr, const double *a, double a_x, double a_y, const double *x, double *y,
+                  double *dot);
+// Per-axis input/output extents of op_id's sweeps and the largest
+// intermediate (elements) of the multi-D product; any output may be null.
+int extents(int op_id, int d, const int *n, const int *bc, int *in, int *out, long long *inter);
 int report(int code, const char *msg);
 int report_cuda(cudaError_t e, const char *what);
 

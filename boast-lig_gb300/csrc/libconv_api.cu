@@ -306,7 +306,8 @@ int plan_md_n(const OpDef &op, int d, const int *n, const int *bc, const int *or
 // Multi-D kinetic, transpose = 0 (Kinetic2.rb:1068-1090), over narr grids
 // laid back to back (narr = 1 is the reference's Kinetic()).
 int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, double a_y,
-             Plan &P, int narr = 1, const int *order = nullptr, bool ekin = false) {
+             Plan &P, int narr = 1, const int *order = nullptr, bool ekin = false,
+             const OpDef &op = OP_D2) {
     if (narr < 1 || narr > 65535) return fail(LIBCONV_EARG, "narr=%d out of [1,65535]", narr);
     if (d < 1 || d > 16) return fail(LIBCONV_EARG, "d=%d out of [1,16]", d);
     if (!n || !bc || !a) return fail(LIBCONV_EARG, "n/bc/a must not be null");
@@ -314,8 +315,8 @@ int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, do
     for (int i = 0; i < d; ++i) {
         if (n[i] < 1) return fail(LIBCONV_EARG, "n[%d]=%d", i, n[i]);
         if (bc[i] != BC_PERIODIC && bc[i] != BC_FREE)
-            return fail(LIBCONV_EBC, "kinetic supports periodic and free (no-grow) only, bc[%d]=%d",
-                        i, bc[i]);
+            return fail(LIBCONV_EBC, "summed 1D sweeps support periodic and free (no-grow) only, "
+                        "bc[%d]=%d", i, bc[i]);
         tot *= n[i];
     }
     if (tot > (1LL << 31) - 1) return fail(LIBCONV_EARG, "grid too large");
@@ -333,7 +334,7 @@ int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, do
         for (int j = 0; j < i; ++j) nL *= n[j];
         for (int j = i + 1; j < d; ++j) nR *= n[j];
         PlanStep st;
-        geometry(OP_D2, bc[i], (int)nL, n[i], (int)nR, n[i], n[i], st.S);
+        geometry(op, bc[i], (int)nL, n[i], (int)nR, n[i], n[i], st.S);
         const bool last = k == d - 1;
         st.S.has_a = 1;
         st.S.a = a[i];
@@ -665,6 +666,89 @@ int kinetic_dotin_sweep(int d, int idim, const int *n, int bc, const int *nx, co
     S.ay_mode = a_y != 0.0 ? 1 : 0;
     S.a_y = a_y;
     S.has_dot = 1;
+    return LIBCONV_OK;
+}
+
+const OpDef *op_of(int id) {
+    switch (id) {
+    case OPID_MD: return &OP_MD;
+    case OPID_IMD: return &OP_IMD;
+    case OPID_D1: return &OP_D1;
+    case OPID_D2: return &OP_D2;
+    case OPID_DWT: return &OP_DWT;
+    case OPID_IWT: return &OP_IWT;
+    case OPID_RTOS1: return &OP_RTOS1;
+    case OPID_S1TOR: return &OP_S1TOR;
+    default: return nullptr;
+    }
+}
+
+// Multi-D product of 1D sweeps (transpose = 1, the dispatcher of
+// GenericConvolution2.rb:1934-2243) with ld, narr, and the scalar options of
+// the Fortran-facing API: y = a (F_{d-1} ... F_0 x) + a_y y, a and a_y on the
+// last sweep; a_x (first sweep in the generated dispatcher, :2040-2043) only
+// for d = 1, where it is y = a F x + a_x x + a_y y.
+int md_generic(int op_id, int d, const int *n, const int *bc, const int *nx, const int *ny,
+               int narr, double a, double a_x, double a_y, const double *x, double *y) {
+    const OpDef *op = op_of(op_id);
+    if (!op) return fail(LIBCONV_EARG, "unknown operator %d", op_id);
+    if (a_x != 0.0 && (d != 1 || op->kind != KCONV))
+        return fail(LIBCONV_EARG, "a_x is defined for one-dimensional convolutions only");
+    Plan P;
+    int rc = plan_md_t(*op, d, n, bc, nx, ny, narr, P);
+    if (rc) return rc;
+    Sweep &S = P.steps.back().S;
+    S.has_a = a != 1.0;
+    S.a = a;
+    S.has_ax = a_x != 0.0;
+    S.a_x = a_x;
+    S.ay_mode = a_y != 0.0 ? 1 : 0;
+    S.a_y = a_y;
+    if (a_y != 0.0) P.y_read = P.elems[B_Y];
+    return exec_host(P, x, y, nullptr);
+}
+
+// Sum of 1D convolutions along every axis (the kinetic form, transpose = 0):
+// y = sum_i a[i] F_i x + a_x x + a_y y, with dot[i] = x . (a[i] F_i x) when
+// dot is not null (host pointers; dot sums over the narr arrays).
+int sum1d_generic(int op_id, int d, const int *n, const int *bc, const int *nx, const int *ny,
+                  int narr, const double *a, double a_x, double a_y, const double *x, double *y,
+                  double *dot) {
+    const OpDef *op = op_of(op_id);
+    if (!op || op->kind != KCONV) return fail(LIBCONV_EARG, "operator %d is not a convolution", op_id);
+    if (n && (nx || ny))
+        for (int i = 0; i < d && i < 16; ++i)
+            if ((nx && nx[i] != n[i]) || (ny && ny[i] != n[i]))
+                return fail(LIBCONV_ESIZE, "summed 1D sweeps need nx = ny = n (axis %d)", i);
+    Plan P;
+    int rc = plan_kin(d, n, bc, a, a_x, a_y, P, narr, nullptr, dot != nullptr, *op);
+    return rc ? rc : exec_host(P, x, y, dot);
+}
+
+// Extents (in the operator's units: pairs for wavelets) that a sweep of
+// op_id with boundary bc reads and writes for n points, and the elements of
+// the largest intermediate of the multi-D product.
+int extents(int op_id, int d, const int *n, const int *bc, int *in, int *out, long long *inter) {
+    const OpDef *op = op_of(op_id);
+    if (!op) return fail(LIBCONV_EARG, "unknown operator %d", op_id);
+    if (d < 1 || d > 16 || !n || !bc) return fail(LIBCONV_EARG, "bad extent arguments");
+    const long long m = nch(*op);
+    long long cur = 1, big = 0;
+    int dims[16];
+    for (int i = 0; i < d; ++i) {
+        if (n[i] < 1) return fail(LIBCONV_EARG, "n[%d]=%d", i, n[i]);
+        if (!bc_valid(bc[i])) return fail(LIBCONV_EBC, "unknown boundary condition %d", bc[i]);
+        dims[i] = need_in(*op, bc[i], n[i]);
+        if (in) in[i] = dims[i];
+        if (out) out[i] = need_out(*op, bc[i], n[i]);
+        cur *= dims[i] * m;
+    }
+    big = cur;
+    for (int i = 0; i < d; ++i) {               // sizes after each sweep
+        cur = cur / (dims[i] * m) * need_out(*op, bc[i], n[i]) * m;
+        if (cur > big) big = cur;
+    }
+    if (inter) *inter = big;
     return LIBCONV_OK;
 }
 

@@ -207,6 +207,27 @@ __device__ __forceinline__ double ll_scaled(long long Y, int se) {
     return ldexp(__longlong_as_double((long long)(sg | (1075ull << 52) | m)), e - 52 + se);
 }
 
+// The same conversion without branches, for the common case: `bad` records
+// a zero-or-subnormal-or-infinite result exponent (the caller then redoes
+// the conversion with ll_scaled).  |Y| is normalised so its leading one is
+// bit 63; bits 10..0 below the 53-bit mantissa give round-to-nearest-even,
+// and a carry out of the mantissa moves into the exponent field.
+__device__ __forceinline__ double ll_scaled_fast(long long Y, int se, bool &bad) {
+    const unsigned long long u = (unsigned long long)Y;
+    const unsigned long long s = (unsigned long long)(Y >> 63);
+    const unsigned long long a = (u ^ s) - s;                    // |Y|
+    const int lz = __clzll((long long)a);                        // 64 when Y == 0
+    const unsigned long long nrm = a << (lz & 63);
+    const unsigned long long mant = nrm >> 11;                   // leading one at bit 52
+    const unsigned long long inc =
+        ((nrm >> 10) & 1ull) & ((unsigned long long)((nrm & 0x3FFull) != 0) | (mant & 1ull));
+    const int be = 1086 - lz + se;                               // exponent field
+    bad |= !(be >= 1 && be <= 2046);
+    const unsigned long long bits =
+        (u & 0x8000000000000000ull) | (((unsigned long long)(be - 1) << 52) + mant + inc);
+    return Y == 0 ? 0.0 : __longlong_as_double((long long)bits);
+}
+
 // Integer value of an FP32 accumulator (an exact integer): one FP32 add of
 // 1.5 * 2^23 leaves it in the low mantissa bits when |v| < 2^22 (ulp 1 in
 // [2^23, 2^24)); `big` records a larger magnitude (the caller then converts
@@ -690,37 +711,58 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
 #pragma unroll
                     for (int n = 0; n < 8; ++n) add[n] = n < nv ? x2step[x2s * n] : 0.0;
                 }
+                // the 8 values of the step first (independent, branch-free
+                // chains; one rare fix-up), then the memory side
+                double outv[8];
+                if (SCH == SCH_EXACT) {
+                    // Y = sum_{k<=5} Acc_k 2^(8(5-k)) + Acc_6 2^-8 (+ Acc_7 2^-16), Horner form
+                    bool big = false, bad = false;
+                    long long Y[8];
+#pragma unroll
+                    for (int n = 0; n < 8; ++n) {
+                        long long v = acc_int(acc[0][n], big);
+#pragma unroll
+                        for (int k = 1; k < 6; ++k) v = v * 256 + acc_int(acc[k][n], big);
+                        int lo = acc_int(acc[6][n], big);
+                        if (G::ORD > 7) lo += (acc_int(acc[G::ORD - 1][n], big) + 128) >> 8;
+                        Y[n] = v + (((long long)lo + 128) >> 8);
+                    }
+                    if (big) {                            // an accumulator >= 2^22: exact path
+#pragma unroll 1
+                        for (int n = 0; n < 8; ++n) {
+                            long long v = __float2int_rn(__uint_as_float(acc[0][n]));
+                            for (int k = 1; k < 6; ++k)
+                                v = v * 256 + __float2int_rn(__uint_as_float(acc[k][n]));
+                            int lo = __float2int_rn(__uint_as_float(acc[6][n]));
+                            if (G::ORD > 7)
+                                lo += (__float2int_rn(__uint_as_float(acc[G::ORD - 1][n])) + 128) >> 8;
+                            Y[n] = v + (((long long)lo + 128) >> 8);
+                        }
+                    }
+#pragma unroll
+                    for (int n = 0; n < 8; ++n) outv[n] = ll_scaled_fast(Y[n], se, bad);
+                    if (bad) {                            // result not a normal number
+#pragma unroll 1
+                        for (int n = 0; n < 8; ++n) outv[n] = ll_scaled(Y[n], se);
+                    }
+                    if (nanrow) {
+#pragma unroll
+                        for (int n = 0; n < 8; ++n) outv[n] = __longlong_as_double(0x7FF8000000000000LL);
+                    }
+                } else {                                  // sum of the order accumulators
+#pragma unroll
+                    for (int n = 0; n < 8; ++n) {
+                        float f = __uint_as_float(acc[0][n]);
+#pragma unroll
+                        for (int k = 1; k < G::ORD; ++k) f += __uint_as_float(acc[k][n]);
+                        outv[n] = f32_to_f64(__float_as_uint(f));
+                    }
+                }
 #pragma unroll
                 for (int n = 0; n < 8; ++n) {
                     const int q = q0 + n / NCH, c = n % NCH;
                     if (n >= nv) break;
-                    double out;
-                    if (SCH == SCH_EXACT) {
-                        // Y = sum_{k<=5} Acc_k 2^(8(5-k)) + Acc_6 2^-8 (+ Acc_7 2^-16), Horner form
-                        bool big = false;
-                        long long Y = acc_int(acc[0][n], big);
-#pragma unroll
-                        for (int k = 1; k < 6; ++k) Y = Y * 256 + acc_int(acc[k][n], big);
-                        int lo = acc_int(acc[6][n], big);
-                        if (G::ORD > 7) lo += (acc_int(acc[G::ORD - 1][n], big) + 128) >> 8;
-                        if (big) {                        // an accumulator >= 2^22: exact path
-                            Y = __float2int_rn(__uint_as_float(acc[0][n]));
-#pragma unroll
-                            for (int k = 1; k < 6; ++k)
-                                Y = Y * 256 + __float2int_rn(__uint_as_float(acc[k][n]));
-                            lo = __float2int_rn(__uint_as_float(acc[6][n]));
-                            if (G::ORD > 7)
-                                lo += (__float2int_rn(__uint_as_float(acc[G::ORD - 1][n])) + 128) >> 8;
-                        }
-                        Y += ((long long)lo + 128) >> 8;
-                        out = nanrow ? __longlong_as_double(0x7FF8000000000000LL)
-                                     : ll_scaled(Y, se);
-                    } else {                              // sum of the order accumulators
-                        float f = __uint_as_float(acc[0][n]);
-#pragma unroll
-                        for (int k = 1; k < G::ORD; ++k) f += __uint_as_float(acc[k][n]);
-                        out = f32_to_f64(__float_as_uint(f));
-                    }
+                    double out = outv[n];
                     double *const yp = ystep + yps * (n / NCH) + ycs * c;
                     if (KIND == KCONV) {
                         const bool want_dot = !BATCH && S.has_dot;   // batched sweeps have no dot

@@ -106,3 +106,38 @@ def test_hamiltonian_sizes_and_validation(pkg):
     with pytest.raises(pkg.LibconvError) as e:
         pkg.hamiltonian_sizes([4, 0, 4], [0, 0, 0])
     assert e.value.status == -1
+
+
+def test_fortran_names_ids_and_sizes(pkg):
+    """Fortran-facing layer, host-only parts: filter / boundary ids and names
+    with blank-padded CHARACTER arguments, the size queries in the order the
+    pipeline calls them (libconv.f90:248-256), and the status word."""
+    F = pkg.Fortran()
+    ids = {nm: F.filter_id(nm) for nm in ('SYM8_LP', 'SYM8_MD', 'SYM8_MI', 'SYM8_D1', 'SYM8_D2',
+                                          'SYMICOMB8')}
+    assert sorted(ids.values()) == [1, 2, 3, 4, 5, 6] and F.status() == 0
+    assert F.filter_id('sym8_md  ') == ids['SYM8_MD']          # case and trailing blanks
+    assert F.filter_id('SYM8_IMD') == ids['SYM8_MI']
+    assert F.filter_name(ids['SYM8_D2']) == 'SYM8_D2'
+    assert F.filter_id('NOPE') == 0 and F.status() == -1
+    assert [F.bc_id(c) for c in 'PGSF'] == [0, 1, -1, 2]
+    assert F.bc_id('fg') == 1 and F.bc_name(-1) == 'S'
+    assert F.bc_id('X') == 0 and F.status() == -2
+    n = [48, 40, 32]
+    lp, md = ids['SYM8_LP'], ids['SYM8_MD']
+    grow, shrink = [1] * 3, [-1] * 3
+    ns0 = F.sizes('get_s1s0_output_size', 3, n, lp, grow)
+    assert ns0 == [v + 7 for v in n]                           # pairs: 2n + 14 points
+    assert F.sizes('get_s1s0_input_size', 3, n, lp, grow) == n
+    assert F.sizes('get_s0s1_input_size', 3, n, lp, shrink) == [v + 7 for v in n]
+    npsir = F.sizes('get_s0s0_md_output_size', 3, [2 * v for v in ns0], md, grow)
+    assert npsir == [2 * v + 15 for v in ns0]
+    assert F.sizes('get_s0s0_md_work_size', 3, [2 * v for v in ns0], md, grow, work=True) >= \
+        2 * int(np.prod(npsir))
+    assert F.sizes('get_s0s0_1ds_output_size', 3, n, ids['SYM8_D2'], [2] * 3) == n
+    with pytest.raises(pkg.LibconvError):
+        F.sizes('get_s0s1_input_size', 3, n, md, shrink)       # not a wavelet filter
+    # tp must be 8; nothing reaches the device
+    st = F.call('s0s0_md', md, 4, 3, n, [0] * 3, n, n, 1, 1.0, 0.0, 0.0, np.zeros(1), np.zeros(1),
+                np.zeros(1), check=False)
+    assert st == -1 and 'tp' in pkg.last_error()
