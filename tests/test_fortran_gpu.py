@@ -42,7 +42,7 @@ def test_s0s0_1d(F, O, fname, oname, bc):
     idim = 1                                     # 0-based axis 1: Fortran idim 2
     nx, ny = list(n), list(n)
     if bc == 1:
-        ny[idim] += 15
+        ny[idim] += 28 if fname == 'SYM8_D1' else 15     # taps - 1
     x = rnd(1, int(np.prod(nx)))
     y0 = rnd(2, int(np.prod(ny)))
     yg, yo = y0.copy(), y0.copy()
