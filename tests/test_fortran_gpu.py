@@ -142,7 +142,7 @@ def test_s0s0_1ds_and_dot(F, O, fname, oname, bc):
     x, y0 = rnd(9, N), rnd(10, N)
     fid = F.filter_id(fname)
     want = 0.4 * x - 0.8 * y0
-    dots = []
+    dots, scale = [], []
     for i in range(3):
         t = np.zeros(N)
         args = [3, i, n, bc[i], n, n, 1, x, t, a[i], 0.0, 0.0]
@@ -153,6 +153,7 @@ def test_s0s0_1ds_and_dot(F, O, fname, oname, bc):
             assert O.call(f'oracle_d_s0s0_1d_sym8_{oname}', *args) == 0
         want = want + t
         dots.append(float(x @ t))
+        scale.append(float(np.abs(x) @ np.abs(t)))   # the D1 dots cancel to rounding noise
     yg = y0.copy()
     F.call('s0s0_1ds', fid, 8, 3, n, bc, n, n, 1, np.array(a), 0.4, -0.8, x, yg, np.zeros(1))
     assert rel(yg, want) <= TOL
@@ -160,7 +161,7 @@ def test_s0s0_1ds_and_dot(F, O, fname, oname, bc):
     F.call('s0s0_1ds_dot', fid, 8, 3, n, bc, n, n, 1, np.array(a), 0.4, -0.8, x, yd, dg,
            np.zeros(1))
     assert rel(yd, want) <= TOL
-    assert np.abs(dg - np.array(dots)).max() <= 1e-12 * np.abs(dots).max()
+    assert np.all(np.abs(dg - np.array(dots)) <= 1e-13 * np.array(scale)), (dg, dots)
     if fname == 'SYM8_D2':
         ye, de = y0.copy(), np.zeros(3)
         F.call('s0s0_1ds_dot_sym8_d2_d', 3, n, bc, n, n, 1, np.array(a), 0.4, -0.8, x, ye, de,
