@@ -1,8 +1,10 @@
 """Build libconv_gb300.so (sm_103a) in-tree with nvcc.
 
 Each translation unit under csrc/ is compiled in parallel to an object file
-under _build/, then linked into ``libconv_gb300.so`` beside this file.  The
-filter header is regenerated first (deterministic; unchanged files are not
+under _build/, then linked into ``libconv_gb300.so`` beside this file and
+archived into ``libconv_gb300.a`` (the same objects, for callers that link
+statically: a Fortran program links it with -lcudart -lstdc++).  The filter
+header is regenerated first (deterministic; unchanged files are not
 rewritten).  Only one -gencode is emitted: sm_103a.
 """
 import concurrent.futures as cf
@@ -14,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'libconv_gb300.so')
+LIBA = os.path.join(HERE, 'libconv_gb300.a')
 NVCC = os.environ.get('NVCC', '/usr/local/cuda/bin/nvcc')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-Wall',
@@ -29,7 +32,8 @@ def _deps_newer(obj, src):
         return True
     t = os.path.getmtime(obj)
     heads = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(('.cuh', '.h'))]
-    heads.append(os.path.join(HERE, '..', 'include', 'libconv_gb300.h'))
+    heads += [os.path.join(HERE, '..', 'include', h)
+              for h in ('libconv_gb300.h', 'libconv_fortran.h')]
     return any(os.path.getmtime(p) > t for p in [src] + heads if os.path.exists(p))
 
 
@@ -56,6 +60,13 @@ def build(verbose=False):
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(LIB + '.tmp', LIB)
+    if not os.path.exists(LIBA) or any(os.path.getmtime(o) > os.path.getmtime(LIBA) for o in objs):
+        if os.path.exists(LIBA + '.tmp'):
+            os.remove(LIBA + '.tmp')
+        r = subprocess.run(['ar', 'rcs', LIBA + '.tmp'] + objs, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"archive failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(LIBA + '.tmp', LIBA)
     if verbose:
         print(f"built {LIB}")
     return LIB

@@ -141,3 +141,47 @@ def test_fortran_names_ids_and_sizes(pkg):
     st = F.call('s0s0_md', md, 4, 3, n, [0] * 3, n, n, 1, 1.0, 0.0, 0.0, np.zeros(1), np.zeros(1),
                 np.zeros(1), check=False)
     assert st == -1 and 'tp' in pkg.last_error()
+
+
+def test_static_library_links_a_fortran_style_caller(pkg, tmp_path):
+    """libconv_gb300.a links into a program that calls the Fortran-facing
+    procedures the way gfortran would (symbols with a trailing underscore,
+    arguments by reference, hidden CHARACTER lengths).  Only the link is
+    checked here (no GPU); the program asks for the filter id and sizes,
+    which need no device."""
+    import os
+    import shutil
+    import subprocess
+    lib_a = os.path.join(os.path.dirname(pkg.LIB_PATH), 'libconv_gb300.a')
+    cc = shutil.which('gcc')
+    if not cc or not os.path.exists(lib_a):
+        pytest.skip('gcc or libconv_gb300.a missing')
+    src = tmp_path / 'caller.c'
+    src.write_text(r'''
+#include <stdio.h>
+#include <stddef.h>
+void get_filter_id_(const char *, int *, size_t);
+void get_s1s0_output_size_(const int *, const int *, const int *, const int *, int *);
+void libconv_status_(int *);
+void s0s0_md_(const int *, const int *, const int *, const int *, const int *, const int *,
+              const int *, const int *, const double *, const double *, const double *,
+              const double *, double *, double *);
+int main(int argc, char **argv) {
+    int fil = 0, st = -99, d = 3, n[3] = {4, 5, 6}, bc[3] = {1, 1, 1}, ns0[3];
+    get_filter_id_("SYM8_LP ", &fil, 8);
+    get_s1s0_output_size_(&d, n, &fil, bc, ns0);
+    libconv_status_(&st);
+    printf("%d %d %d %d %d\n", fil, st, ns0[0], ns0[1], ns0[2]);
+    if (argc > 5) s0s0_md_(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0);   /* referenced only */
+    return 0;
+}
+''')
+    cuda_lib = '/usr/local/cuda/lib64'
+    exe = tmp_path / 'caller'
+    r = subprocess.run([cc, str(src), lib_a, '-L' + cuda_lib, '-lcudart', '-lstdc++', '-lm',
+                        '-lpthread', '-ldl', '-o', str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    run = subprocess.run([str(exe)], capture_output=True, text=True,
+                         env={**os.environ, 'LD_LIBRARY_PATH': cuda_lib})
+    assert run.returncode == 0, run.stderr
+    assert run.stdout.split() == ['1', '0', '11', '12', '13']
