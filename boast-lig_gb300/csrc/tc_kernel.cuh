@@ -713,52 +713,77 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                 }
                 if constexpr (G::ORD > 7) {
                     // 8 order accumulators (29-tap filters, combined wavelets):
-                    // convert and store output by output (register budget)
-    #pragma unroll
-                    for (int n = 0; n < 8; ++n) {
-                        const int q = q0 + n / NCH, c = n % NCH;
-                        if (n >= nv) break;
-                        double out;
+                    // the same two phases, 4 outputs at a time (register budget)
+#pragma unroll
+                    for (int g0 = 0; g0 < 8; g0 += 4) {
+                        if (g0 >= nv) continue;
+                        double outv[4];
                         if (SCH == SCH_EXACT) {
-                            // Y = sum_{k<=5} Acc_k 2^(8(5-k)) + Acc_6 2^-8 (+ Acc_7 2^-16), Horner form
-                            bool big = false;
-                            long long Y = acc_int(acc[0][n], big);
-    #pragma unroll
-                            for (int k = 1; k < 6; ++k) Y = Y * 256 + acc_int(acc[k][n], big);
-                            int lo = acc_int(acc[6][n], big);
-                            if (G::ORD > 7) lo += (acc_int(acc[G::ORD - 1][n], big) + 128) >> 8;
-                            if (big) {                        // an accumulator >= 2^22: exact path
-                                Y = __float2int_rn(__uint_as_float(acc[0][n]));
-    #pragma unroll
-                                for (int k = 1; k < 6; ++k)
-                                    Y = Y * 256 + __float2int_rn(__uint_as_float(acc[k][n]));
-                                lo = __float2int_rn(__uint_as_float(acc[6][n]));
-                                if (G::ORD > 7)
+                            bool big = false, bad = false;
+                            long long Y[4];
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) {
+                                const int n = g0 + i;
+                                long long v = acc_int(acc[0][n], big);
+#pragma unroll
+                                for (int k = 1; k < 6; ++k) v = v * 256 + acc_int(acc[k][n], big);
+                                int lo = acc_int(acc[6][n], big);
+                                lo += (acc_int(acc[G::ORD - 1][n], big) + 128) >> 8;
+                                Y[i] = v + (((long long)lo + 128) >> 8);
+                            }
+                            if (big) {                    // an accumulator >= 2^22: exact path
+#pragma unroll
+                                for (int i = 0; i < 4; ++i) {
+                                    const int n = g0 + i;
+                                    long long v = __float2int_rn(__uint_as_float(acc[0][n]));
+#pragma unroll
+                                    for (int k = 1; k < 6; ++k)
+                                        v = v * 256 + __float2int_rn(__uint_as_float(acc[k][n]));
+                                    int lo = __float2int_rn(__uint_as_float(acc[6][n]));
                                     lo += (__float2int_rn(__uint_as_float(acc[G::ORD - 1][n])) + 128) >> 8;
+                                    Y[i] = v + (((long long)lo + 128) >> 8);
+                                }
                             }
-                            Y += ((long long)lo + 128) >> 8;
-                            out = nanrow ? __longlong_as_double(0x7FF8000000000000LL)
-                                         : ll_scaled(Y, se);
-                        } else {                              // sum of the order accumulators
-                            float f = __uint_as_float(acc[0][n]);
-    #pragma unroll
-                            for (int k = 1; k < G::ORD; ++k) f += __uint_as_float(acc[k][n]);
-                            out = f32_to_f64(__float_as_uint(f));
-                        }
-                        double *const yp = ystep + yps * (n / NCH) + ycs * c;
-                        if (KIND == KCONV) {
-                            const bool want_dot = !BATCH && S.has_dot;   // batched sweeps have no dot
-                            if ((want_dot || S.has_ax) && (!grow || (q >= 0 && q < S.n))) {
-                                const int ps = S.bc == BC_PERIODIC ? imod(q, S.n) : q - S.in_lo;
-                                const double xq = xrow[(long long)S.nL * ps];
-                                if (want_dot) dot = fma(xq, out, dot);
-                                if (S.has_ax) out = fma(xq, S.a_x, out);
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) outv[i] = ll_scaled_fast(Y[i], se, bad);
+                            if (bad) {                    // result not a normal number
+#pragma unroll
+                                for (int i = 0; i < 4; ++i) outv[i] = ll_scaled(Y[i], se);
                             }
-                            if (x2) out += add[n];
+                            if (nanrow) {
+#pragma unroll
+                                for (int i = 0; i < 4; ++i) outv[i] = __longlong_as_double(0x7FF8000000000000LL);
+                            }
+                        } else {                          // sum of the order accumulators
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) {
+                                float f = __uint_as_float(acc[0][g0 + i]);
+#pragma unroll
+                                for (int k = 1; k < G::ORD; ++k) f += __uint_as_float(acc[k][g0 + i]);
+                                outv[i] = f32_to_f64(__float_as_uint(f));
+                            }
                         }
-                        if (S.ay_mode == 2) out += *yp;
-                        else if (S.ay_mode == 1) out = fma(S.a_y, *yp, out);
-                        *yp = out;
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            const int n = g0 + i;
+                            const int q = q0 + n / NCH, c = n % NCH;
+                            if (n >= nv) break;
+                            double out = outv[i];
+                            double *const yp = ystep + yps * (n / NCH) + ycs * c;
+                            if (KIND == KCONV) {
+                                const bool want_dot = !BATCH && S.has_dot;   // batched sweeps have no dot
+                                if ((want_dot || S.has_ax) && (!grow || (q >= 0 && q < S.n))) {
+                                    const int ps = S.bc == BC_PERIODIC ? imod(q, S.n) : q - S.in_lo;
+                                    const double xq = xrow[(long long)S.nL * ps];
+                                    if (want_dot) dot = fma(xq, out, dot);
+                                    if (S.has_ax) out = fma(xq, S.a_x, out);
+                                }
+                                if (x2) out += add[n];
+                            }
+                            if (S.ay_mode == 2) out += *yp;
+                            else if (S.ay_mode == 1) out = fma(S.a_y, *yp, out);
+                            *yp = out;
+                        }
                     }
                 } else {
                     // 7 order accumulators: the 8 values of the step first
