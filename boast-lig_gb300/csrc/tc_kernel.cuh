@@ -711,9 +711,9 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
 #pragma unroll
                     for (int n = 0; n < 8; ++n) add[n] = n < nv ? x2step[x2s * n] : 0.0;
                 }
-                if constexpr (G::ORD > 7) {
-                    // 8 order accumulators (29-tap filters, combined wavelets):
-                    // the same two phases, 4 outputs at a time (register budget)
+                {
+                    // 4 outputs at a time: their values first (independent,
+                    // branch-free chains; one rare fix-up), then their memory side
 #pragma unroll
                     for (int g0 = 0; g0 < 8; g0 += 4) {
                         if (g0 >= nv) continue;
@@ -728,7 +728,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
 #pragma unroll
                                 for (int k = 1; k < 6; ++k) v = v * 256 + acc_int(acc[k][n], big);
                                 int lo = acc_int(acc[6][n], big);
-                                lo += (acc_int(acc[G::ORD - 1][n], big) + 128) >> 8;
+                                if (G::ORD > 7) lo += (acc_int(acc[G::ORD - 1][n], big) + 128) >> 8;
                                 Y[i] = v + (((long long)lo + 128) >> 8);
                             }
                             if (big) {                    // an accumulator >= 2^22: exact path
@@ -740,7 +740,8 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                                     for (int k = 1; k < 6; ++k)
                                         v = v * 256 + __float2int_rn(__uint_as_float(acc[k][n]));
                                     int lo = __float2int_rn(__uint_as_float(acc[6][n]));
-                                    lo += (__float2int_rn(__uint_as_float(acc[G::ORD - 1][n])) + 128) >> 8;
+                                    if (G::ORD > 7)
+                                        lo += (__float2int_rn(__uint_as_float(acc[G::ORD - 1][n])) + 128) >> 8;
                                     Y[i] = v + (((long long)lo + 128) >> 8);
                                 }
                             }
@@ -784,76 +785,6 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                             else if (S.ay_mode == 1) out = fma(S.a_y, *yp, out);
                             *yp = out;
                         }
-                    }
-                } else {
-                    // 7 order accumulators: the 8 values of the step first
-                    // (independent, branch-free chains), then the memory side
-                    // the 8 values of the step first (independent, branch-free
-                    // chains; one rare fix-up), then the memory side
-                    double outv[8];
-                    if (SCH == SCH_EXACT) {
-                        // Y = sum_{k<=5} Acc_k 2^(8(5-k)) + Acc_6 2^-8 (+ Acc_7 2^-16), Horner form
-                        bool big = false, bad = false;
-                        long long Y[8];
-    #pragma unroll
-                        for (int n = 0; n < 8; ++n) {
-                            long long v = acc_int(acc[0][n], big);
-    #pragma unroll
-                            for (int k = 1; k < 6; ++k) v = v * 256 + acc_int(acc[k][n], big);
-                            int lo = acc_int(acc[6][n], big);
-                            if (G::ORD > 7) lo += (acc_int(acc[G::ORD - 1][n], big) + 128) >> 8;
-                            Y[n] = v + (((long long)lo + 128) >> 8);
-                        }
-                        if (big) {                            // an accumulator >= 2^22: exact path
-    #pragma unroll
-                            for (int n = 0; n < 8; ++n) {
-                                long long v = __float2int_rn(__uint_as_float(acc[0][n]));
-                                for (int k = 1; k < 6; ++k)
-                                    v = v * 256 + __float2int_rn(__uint_as_float(acc[k][n]));
-                                int lo = __float2int_rn(__uint_as_float(acc[6][n]));
-                                if (G::ORD > 7)
-                                    lo += (__float2int_rn(__uint_as_float(acc[G::ORD - 1][n])) + 128) >> 8;
-                                Y[n] = v + (((long long)lo + 128) >> 8);
-                            }
-                        }
-    #pragma unroll
-                        for (int n = 0; n < 8; ++n) outv[n] = ll_scaled_fast(Y[n], se, bad);
-                        if (bad) {                            // result not a normal number
-    #pragma unroll
-                            for (int n = 0; n < 8; ++n) outv[n] = ll_scaled(Y[n], se);
-                        }
-                        if (nanrow) {
-    #pragma unroll
-                            for (int n = 0; n < 8; ++n) outv[n] = __longlong_as_double(0x7FF8000000000000LL);
-                        }
-                    } else {                                  // sum of the order accumulators
-    #pragma unroll
-                        for (int n = 0; n < 8; ++n) {
-                            float f = __uint_as_float(acc[0][n]);
-    #pragma unroll
-                            for (int k = 1; k < G::ORD; ++k) f += __uint_as_float(acc[k][n]);
-                            outv[n] = f32_to_f64(__float_as_uint(f));
-                        }
-                    }
-    #pragma unroll
-                    for (int n = 0; n < 8; ++n) {
-                        const int q = q0 + n / NCH, c = n % NCH;
-                        if (n >= nv) break;
-                        double out = outv[n];
-                        double *const yp = ystep + yps * (n / NCH) + ycs * c;
-                        if (KIND == KCONV) {
-                            const bool want_dot = !BATCH && S.has_dot;   // batched sweeps have no dot
-                            if ((want_dot || S.has_ax) && (!grow || (q >= 0 && q < S.n))) {
-                                const int ps = S.bc == BC_PERIODIC ? imod(q, S.n) : q - S.in_lo;
-                                const double xq = xrow[(long long)S.nL * ps];
-                                if (want_dot) dot = fma(xq, out, dot);
-                                if (S.has_ax) out = fma(xq, S.a_x, out);
-                            }
-                            if (x2) out += add[n];
-                        }
-                        if (S.ay_mode == 2) out += *yp;
-                        else if (S.ay_mode == 1) out = fma(S.a_y, *yp, out);
-                        *yp = out;
                     }
                 }
             }
