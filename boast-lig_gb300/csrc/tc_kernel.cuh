@@ -228,6 +228,31 @@ __device__ __forceinline__ double ll_scaled_fast(long long Y, int se, bool &bad)
     return Y == 0 ? 0.0 : __longlong_as_double((long long)bits);
 }
 
+// Bits of an FP32 accumulator plus 1.5 * 2^23 (the integer sits in the low
+// mantissa bits, biased by 0x4B400000, when |v| < 2^22; `big` records a
+// larger magnitude).
+__device__ __forceinline__ uint32_t acc_bits(uint32_t u, bool &big) {
+    const float f = __uint_as_float(u);
+    big |= !(fabsf(f) < 4194304.0f);
+    return __float_as_uint(f + 12582912.0f);
+}
+
+// sum_{k<6} v_k 2^(8(5-k)) from the biased bits b_k = v_k + 0x4B400000 of
+// acc_bits: Horner modulo 2^64 on the biased bits (three 32x32+64
+// multiply-adds for the low terms, one 32-bit add into the high word for
+// the two top terms), then the bias of all six terms removed at once.  The
+// wrap-around is exact because the true sum fits in 64 bits.
+__device__ __forceinline__ long long horner6(const uint32_t (&b)[6]) {
+    constexpr unsigned long long kBias =
+        0x4B400000ull * ((1ull << 40) + (1ull << 32) + (1ull << 24) + (1ull << 16) + (1ull << 8) + 1ull);
+    unsigned long long v = b[5];
+    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(v) : "r"(b[4]), "r"(256u), "l"(v));
+    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(v) : "r"(b[3]), "r"(65536u), "l"(v));
+    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(v) : "r"(b[2]), "r"(16777216u), "l"(v));
+    v += (unsigned long long)(b[1] + (b[0] << 8)) << 32;
+    return (long long)(v - kBias);
+}
+
 // Integer value of an FP32 accumulator (an exact integer): one FP32 add of
 // 1.5 * 2^23 leaves it in the low mantissa bits when |v| < 2^22 (ulp 1 in
 // [2^23, 2^24)); `big` records a larger magnitude (the caller then converts
@@ -724,9 +749,10 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
 #pragma unroll
                             for (int i = 0; i < 4; ++i) {
                                 const int n = g0 + i;
-                                long long v = acc_int(acc[0][n], big);
+                                uint32_t bb[6];
 #pragma unroll
-                                for (int k = 1; k < 6; ++k) v = v * 256 + acc_int(acc[k][n], big);
+                                for (int k = 0; k < 6; ++k) bb[k] = acc_bits(acc[k][n], big);
+                                const long long v = horner6(bb);
                                 int lo = acc_int(acc[6][n], big);
                                 if (G::ORD > 7) lo += (acc_int(acc[G::ORD - 1][n], big) + 128) >> 8;
                                 Y[i] = v + (((long long)lo + 128) >> 8);
