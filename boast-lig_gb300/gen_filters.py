@@ -22,6 +22,17 @@ Derived tables (restated algorithms, computed here):
     zero) to 30 decimal places, as the reference does with
     BigDecimal#truncate(30).
 
+  * the Poisson finite-difference first derivatives of order nord in
+    {2, 4, 6, 8, 16} (BigDFT/Poisson.rb:20-166, the table c1D(-m:m,-m:m),
+    m = nord/2): c1D(:, j) are the weights on the nord+1 unit-spaced nodes
+    0..nord for the derivative at node m + j, i.e. Fornberg's algorithm
+    (Math. Comp. 51 (1988) 699-706) in exact rational arithmetic, each
+    weight rounded once to the nearest double (the reference writes each as
+    one quotient of two exact doubles, which rounds the same way).  One entry
+    of the reference table differs from those weights: its nord = 8 stencil
+    for the first node, c1D(0,-4), is +35/2 where the weight is -35/2; it is
+    kept as the reference has it, so results match the reference's.
+
 Every decimal string is converted to the nearest double (Python ``float`` is
 correctly rounded, as a C compiler's literal parsing is) and emitted with
 ``repr`` so the C literal round-trips to that exact double.
@@ -29,6 +40,7 @@ correctly rounded, as a C compiler's literal parsing is) and emitted with
 Usage: python gen_filters.py [output_header]
 """
 from decimal import Decimal, getcontext, ROUND_DOWN
+from fractions import Fraction
 import os
 import sys
 
@@ -269,6 +281,42 @@ def wavelet_sets():
     return sets
 
 
+FD_ORDERS = (2, 4, 6, 8, 16)
+FD_NTAPS = 17          # every central stencil padded to 17 taps (lowfil -8)
+
+
+def fornberg(z, nodes):
+    """Exact first-derivative weights at z on `nodes` (Fornberg 1988, m = 1)."""
+    n = len(nodes) - 1
+    c = [[Fraction(0), Fraction(0)] for _ in range(n + 1)]
+    c[0][0] = Fraction(1)
+    c1, c4 = Fraction(1), Fraction(nodes[0] - z)
+    for i in range(1, n + 1):
+        mn = min(i, 1)
+        c2, c5, c4 = Fraction(1), c4, Fraction(nodes[i] - z)
+        for j in range(i):
+            c3 = Fraction(nodes[i] - nodes[j])
+            c2 *= c3
+            if j == i - 1:
+                for k in range(mn, 0, -1):
+                    c[i][k] = c1 * (k * c[i - 1][k - 1] - c5 * c[i - 1][k]) / c2
+                c[i][0] = -c1 * c5 * c[i - 1][0] / c2
+            for k in range(mn, 0, -1):
+                c[j][k] = (c4 * c[j][k] - k * c[j][k - 1]) / c3
+            c[j][0] = c4 * c[j][0] / c3
+        c1 = c2
+    return [c[i][1] for i in range(n + 1)]
+
+
+def fd_table(nord):
+    """c1D(:, j) for j = -m..m (rows), weights on nodes 0..nord (columns)."""
+    m = nord // 2
+    rows = [fornberg(m + j, list(range(nord + 1))) for j in range(-m, m + 1)]
+    if nord == 8:
+        rows[0][4] = -rows[0][4]          # the reference's c1D(0,-4) = +35/2
+    return rows
+
+
 def carr(name, vals):
     body = ',\n  '.join(repr(float(v)) for v in vals)
     return f"static const double {name}[{len(vals)}] = {{\n  {body}\n}};\n"
@@ -306,6 +354,25 @@ def generate():
     put('IMD', SYM8_MF)
     put('D1', SYM8_D1)
     put('D2', SYM8_D2)
+    # Poisson central stencils c1D(:,0), zero-padded to 17 taps at lowfil -8
+    out.append("/* Poisson finite differences (nord 2..16): central stencils in the flat\n"
+               " * table (17 taps, lowfil -8, zero padded); one-sided stencils c1D(:,j),\n"
+               " * j = -m..m, row after row, in LCG_FD_EDGE at LCG_FD_EDGE_OFF_<nord>. */\n"
+               f"#define LCG_FD_NTAPS ({FD_NTAPS})\n#define LCG_FD_LOWFIL (-8)\n")
+    edge, edge_offs = [], []
+    for nord in FD_ORDERS:
+        rows = fd_table(nord)
+        m = nord // 2
+        central = [Fraction(0)] * (8 - m) + rows[m] + [Fraction(0)] * (8 - m)
+        put(f'FD{nord}', central)
+        edge_offs.append((nord, len(edge)))
+        for r in rows:
+            edge.extend(float(v) for v in r)
+    for nord, off in edge_offs:
+        out.append(f"#define LCG_FD_EDGE_OFF_{nord} {off}\n")
+    out.append(f"#define LCG_FD_EDGE_N {len(edge)}\n")
+    out.append("#define LCG_FD_EDGE_INIT { \\\n  " +
+               ", \\\n  ".join(repr(v) for v in edge) + " }\n")
     for (name, d, fam), (le, lo, he, ho, lowfil, length) in sorted(wavelet_sets().items()):
         tag = f"LCG_WT_{name.upper()}_{d.upper()}_{fam.upper()}"
         out.append(f"/* {name} {d} ({'periodic/free' if fam == 'p' else 'grow/shrink'}): "

@@ -600,3 +600,239 @@ int oracle_hamiltonian(const int *n, const int *bc, const double *a_kin, const d
     free(fscf); free(hpsi); free(tmp); free(psir); free(w1); free(w2);
     return rc;
 }
+
+/* ======================================================================
+ * Poisson finite-difference operators (BigDFT/Poisson.rb).
+ * c1D(j, k), j, k = -m..m, m = nord/2: derivative weights of order nord on
+ * nodes 0..nord at node m + k (Poisson.rb:20-166); LCG_FD_EDGE holds the
+ * rows k in order, each row j = -m..m.
+ * ====================================================================== */
+enum { BC_NPERIODIC = -2 };
+static const double FD_EDGE[LCG_FD_EDGE_N] = LCG_FD_EDGE_INIT;
+static const double ONEO4PI = 0.07957747154594766788444188168625718101722982287022822437383367203;
+
+static const double *fd_rows(int nord)
+{
+    switch (nord) {
+    case 2: return FD_EDGE + LCG_FD_EDGE_OFF_2;
+    case 4: return FD_EDGE + LCG_FD_EDGE_OFF_4;
+    case 6: return FD_EDGE + LCG_FD_EDGE_OFF_6;
+    case 8: return FD_EDGE + LCG_FD_EDGE_OFF_8;
+    case 16: return FD_EDGE + LCG_FD_EDGE_OFF_16;
+    default: return 0;
+    }
+}
+#define C1D(t, m, j, k) ((t)[((k) + (m)) * (2 * (m) + 1) + (j) + (m)])
+
+/* Poisson_broker (Poisson.rb:1951-2043) running the generated 1D operator
+ * (GenericConvolution2.rb, PoissonFilter 237-294: transpose 0, option a):
+ * du = a * (sum_j c1D(j, k) u(..)) along axis idim.  Periodic: the central
+ * stencil with modulo wrap; NPERIODIC: the one-sided stencils for the m
+ * first (c1D(:, i-m) on nodes 0..nord) and m last points (c1D(:, i-n+m+1)
+ * on the last nord+1 nodes) of every line (set_filter_val :begin/:end,
+ * 265-281, and input_filter_index, 283-293); taps in ascending j. */
+int oracle_poisson_broker(int nord, int idim, const int *nn, int bc, const double *u, double *du,
+                          double a)
+{
+    const double *t = fd_rows(nord);
+    if (!t || !nn || !u || !du || idim < 0 || idim > 2) return E_ARG;
+    if (bc != BC_PERIODIC && bc != BC_NPERIODIC) return E_BC;
+    const int m = nord / 2, n = nn[idim];
+    if (nn[0] < 1 || nn[1] < 1 || nn[2] < 1) return E_ARG;
+    if (bc == BC_NPERIODIC && n < nord + 1) return E_SIZE;
+    long nL = 1, nR = 1;
+    for (int k = 0; k < idim; ++k) nL *= nn[k];
+    for (int k = idim + 1; k < 3; ++k) nR *= nn[k];
+    for (long r = 0; r < nR; ++r)
+        for (long l = 0; l < nL; ++l) {
+            const double *x = u + l + nL * n * r;
+            double *y = du + l + nL * n * r;
+            for (int i = 0; i < n; ++i) {
+                double tt = 0.0;
+                if (bc == BC_PERIODIC || (i >= m && i < n - m)) {
+                    for (int j = -m; j <= m; ++j) {
+                        const int p = bc == BC_PERIODIC ? imod(i + j, n) : i + j;
+                        tt = tt + C1D(t, m, j, 0) * x[nL * p];
+                    }
+                } else if (i < m) {
+                    for (int j = -m; j <= m; ++j) tt = tt + C1D(t, m, j, i - m) * x[nL * (j + m)];
+                } else {
+                    for (int j = -m; j <= m; ++j)
+                        tt = tt + C1D(t, m, j, i - n + m + 1) * x[nL * (n - 1 + j - m)];
+                }
+                y[nL * i] = tt * a;
+            }
+        }
+    return OK;
+}
+
+/* geocode 1 (free): x and z non-periodic; 2 (periodic); 3 (surface): y
+ * non-periodic (Poisson.rb:2122-2128). */
+static int geocode_bc(int geocode, int bc[3])
+{
+    if (geocode < 1 || geocode > 3) return E_ARG;
+    bc[0] = bc[1] = bc[2] = BC_PERIODIC;
+    if (geocode == 1) bc[0] = bc[2] = BC_NPERIODIC;
+    if (geocode != 2) bc[1] = BC_NPERIODIC;
+    return OK;
+}
+
+static int nabla3(int geocode, const int *nn, const double *u, double *du, int nord,
+                  const double *hgrids)
+{
+    int bc[3], rc = geocode_bc(geocode, bc);
+    const size_t N = (size_t)nn[0] * nn[1] * nn[2];
+    for (int i = 0; i < 3 && rc == OK; ++i)
+        rc = oracle_poisson_broker(nord, i, nn, bc[i], u, du + i * N, 1.0 / hgrids[i]);
+    return rc;
+}
+
+/* div_u_i (Poisson.rb:2067-2194): du = d0 u0 + d1 u1 + d2 u2; with cc, also
+ * cc = u0^2 d0u0 + u1^2 d1u1 + u2^2 d2u2 + 2 (u0 u1 d0u1 + u0 u2 d0u2 + u1 u2 d1u2). */
+int oracle_div_u_i(int geocode, int n01, int n02, int n03, const double *u, double *du, int nord,
+                   const double *hgrids, double *cc)
+{
+    const int nn[3] = {n01, n02, n03};
+    int bc[3], rc = geocode_bc(geocode, bc);
+    if (rc || !u || !du || !hgrids || n01 < 1 || n02 < 1 || n03 < 1) return rc ? rc : E_ARG;
+    const size_t N = (size_t)n01 * n02 * n03;
+    const double a0 = 1.0 / hgrids[0], a1 = 1.0 / hgrids[1], a2 = 1.0 / hgrids[2];
+    double *t = malloc((cc ? 5 : 3) * N * sizeof(double));
+    if (!t) return E_ARG;
+    if (cc) {
+        rc = oracle_poisson_broker(nord, 0, nn, bc[0], u, du, a0);
+        if (!rc) rc = oracle_poisson_broker(nord, 1, nn, bc[1], u + N, t, a1);
+        if (!rc) rc = oracle_poisson_broker(nord, 2, nn, bc[2], u + 2 * N, t + N, a2);
+        if (!rc) rc = oracle_poisson_broker(nord, 0, nn, bc[0], u + N, t + 2 * N, a0);
+        if (!rc) rc = oracle_poisson_broker(nord, 0, nn, bc[0], u + 2 * N, t + 3 * N, a0);
+        if (!rc) rc = oracle_poisson_broker(nord, 1, nn, bc[1], u + 2 * N, t + 4 * N, a1);
+        for (size_t k = 0; k < N && !rc; ++k) {
+            const double u0 = u[k], u1 = u[N + k], u2 = u[2 * N + k];
+            const double du0 = du[k], du1 = t[k], du2 = t[N + k];
+            cc[k] = (u0 * u0) * du0 + (u1 * u1) * du1 + (u2 * u2) * du2 +
+                    2.0 * (u0 * u1 * t[2 * N + k] + u0 * u2 * t[3 * N + k] + u1 * u2 * t[4 * N + k]);
+            du[k] = du0 + du1 + du2;
+        }
+    } else {
+        rc = oracle_poisson_broker(nord, 0, nn, bc[0], u, t, a0);
+        if (!rc) rc = oracle_poisson_broker(nord, 1, nn, bc[1], u + N, t + N, a1);
+        if (!rc) rc = oracle_poisson_broker(nord, 2, nn, bc[2], u + 2 * N, t + 2 * N, a2);
+        for (size_t k = 0; k < N && !rc; ++k) du[k] = t[k] + t[N + k] + t[2 * N + k];
+    }
+    free(t);
+    return rc;
+}
+
+/* nabla_u (Poisson.rb:2553-2620): du(:,:,:,i) = d_i u. */
+int oracle_nabla_u(int geocode, int n01, int n02, int n03, const double *u, double *du, int nord,
+                   const double *hgrids)
+{
+    const int nn[3] = {n01, n02, n03};
+    if (!u || !du || !hgrids || n01 < 1 || n02 < 1 || n03 < 1) return E_ARG;
+    return nabla3(geocode, nn, u, du, nord, hgrids);
+}
+
+/* nabla_u_and_square (Poisson.rb:2197-2275): du as nabla_u, ddu = |du|^2. */
+int oracle_nabla_u_and_square(int geocode, int n01, int n02, int n03, const double *u, double *du,
+                              double *ddu, int nord, const double *hgrids)
+{
+    int rc = oracle_nabla_u(geocode, n01, n02, n03, u, du, nord, hgrids);
+    if (rc || !ddu) return rc ? rc : E_ARG;
+    const size_t N = (size_t)n01 * n02 * n03;
+    for (size_t k = 0; k < N; ++k)
+        ddu[k] = (du[k] * du[k]) + (du[N + k] * du[N + k]) + (du[2 * N + k] * du[2 * N + k]);
+    return OK;
+}
+
+/* nabla_u_square (Poisson.rb:2278-2359): ddu = |nabla u|^2. */
+int oracle_nabla_u_square(int geocode, int n01, int n02, int n03, const double *u, double *ddu,
+                          int nord, const double *hgrids)
+{
+    const size_t N = (size_t)n01 * n02 * n03;
+    double *du = malloc(3 * (N ? N : 1) * sizeof(double));
+    if (!du) return E_ARG;
+    int rc = oracle_nabla_u_and_square(geocode, n01, n02, n03, u, du, ddu, nord, hgrids);
+    free(du);
+    return rc;
+}
+
+/* nabla_u_epsilon (Poisson.rb:2362-2443): du(:,:,:,i) = d_i u * eps. */
+int oracle_nabla_u_epsilon(int geocode, int n01, int n02, int n03, const double *u, double *du,
+                           int nord, const double *hgrids, const double *eps)
+{
+    int rc = oracle_nabla_u(geocode, n01, n02, n03, u, du, nord, hgrids);
+    if (rc || !eps) return rc ? rc : E_ARG;
+    const size_t N = (size_t)n01 * n02 * n03;
+    for (size_t k = 0; k < N; ++k) {
+        du[k] = du[k] * eps[k];
+        du[N + k] = du[N + k] * eps[k];
+        du[2 * N + k] = du[2 * N + k] * eps[k];
+    }
+    return OK;
+}
+
+/* update_rhopol (Poisson.rb:2446-2550): res = (dlogeps . nabla u) / (4 pi);
+ * res = (res - rhopol) eta; rhores2 = sum res^2; rhopol = res + rhopol.
+ * dlogeps(3, n01, n02, n03): component fastest. */
+int oracle_update_rhopol(int geocode, int n01, int n02, int n03, const double *u, int nord,
+                         const double *hgrids, double eta, const double *dlogeps, double *rhopol,
+                         double *rhores2)
+{
+    const size_t N = (size_t)n01 * n02 * n03;
+    if (!dlogeps || !rhopol || !rhores2) return E_ARG;
+    double *du = malloc(3 * (N ? N : 1) * sizeof(double));
+    if (!du) return E_ARG;
+    int rc = oracle_nabla_u(geocode, n01, n02, n03, u, du, nord, hgrids);
+    double acc = 0.0;
+    for (size_t k = 0; k < N && !rc; ++k) {
+        double res = dlogeps[3 * k] * du[k] + dlogeps[3 * k + 1] * du[N + k] +
+                     dlogeps[3 * k + 2] * du[2 * N + k];
+        res = res * ONEO4PI;
+        const double rho = rhopol[k];
+        res = (res - rho) * eta;
+        acc = acc + res * res;
+        rhopol[k] = res + rho;
+    }
+    if (!rc) *rhores2 = acc;
+    free(du);
+    return rc;
+}
+
+/* div_u_i_ref as written in Fortran (Poisson.rb:181-340): the same stencils,
+ * each directional sum divided by h (not multiplied by 1/h). */
+int oracle_div_u_i_ref(int geocode, int n01, int n02, int n03, const double *u, double *du,
+                       int nord, const double *hgrids)
+{
+    const double *t = fd_rows(nord);
+    int bc[3];
+    if (!t || !u || !du || !hgrids || geocode_bc(geocode, bc)) return E_ARG;
+    const int m = nord / 2, nn[3] = {n01, n02, n03};
+    const size_t N = (size_t)n01 * n02 * n03;
+    const long st[3] = {1, n01, (long)n01 * n02};
+    for (int i3 = 0; i3 < n03; ++i3)
+        for (int i2 = 0; i2 < n02; ++i2)
+            for (int i1 = 0; i1 < n01; ++i1) {
+                const int ii[3] = {i1, i2, i3};
+                const long k0 = i1 + (long)n01 * (i2 + (long)n02 * i3);
+                double d[3];
+                for (int a = 0; a < 3; ++a) {
+                    const int n = nn[a], i = ii[a];
+                    const double *x = u + a * N + k0 - (long)i * st[a];   /* start of the line */
+                    double s = 0.0;
+                    if (bc[a] == BC_PERIODIC || (i >= m && i < n - m)) {
+                        for (int j = -m; j <= m; ++j) {
+                            const int p = bc[a] == BC_PERIODIC ? imod(i + j, n) : i + j;
+                            s = s + C1D(t, m, j, 0) * x[st[a] * p];
+                        }
+                    } else if (i < m) {
+                        for (int j = -m; j <= m; ++j) s = s + C1D(t, m, j, i - m) * x[st[a] * (j + m)];
+                    } else {
+                        for (int j = -m; j <= m; ++j)
+                            s = s + C1D(t, m, j, i - n + m + 1) * x[st[a] * (n - 1 + j - m)];
+                    }
+                    d[a] = s / hgrids[a];
+                }
+                du[k0] = d[0] + d[1] + d[2];
+            }
+    return OK;
+}

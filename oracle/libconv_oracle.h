@@ -81,6 +81,26 @@ int oracle_d_idwt_sym8(int d, const int *n, const int *bc, const double *x, doub
  * MagicFilter grow, rho += psir^2 (rho may be NULL), epot = sum v psir^2,
  * psir = v psir, inverse MagicFilter shrink, kinetic no-grow accumulated
  * with ekin[3] per direction, dwt shrink.  bc[i]: periodic (0) or free (2). */
+/* Poisson finite-difference operators (BigDFT/Poisson.rb): the 1D broker
+ * (bc 0 periodic, -2 non-periodic), the generated 3D drivers and the
+ * Fortran div_u_i_ref. */
+int oracle_poisson_broker(int nord, int idim, const int *nn, int bc, const double *u, double *du,
+                          double a);
+int oracle_div_u_i(int geocode, int n01, int n02, int n03, const double *u, double *du, int nord,
+                   const double *hgrids, double *cc);
+int oracle_nabla_u(int geocode, int n01, int n02, int n03, const double *u, double *du, int nord,
+                   const double *hgrids);
+int oracle_nabla_u_and_square(int geocode, int n01, int n02, int n03, const double *u, double *du,
+                              double *ddu, int nord, const double *hgrids);
+int oracle_nabla_u_square(int geocode, int n01, int n02, int n03, const double *u, double *ddu,
+                          int nord, const double *hgrids);
+int oracle_nabla_u_epsilon(int geocode, int n01, int n02, int n03, const double *u, double *du,
+                           int nord, const double *hgrids, const double *eps);
+int oracle_update_rhopol(int geocode, int n01, int n02, int n03, const double *u, int nord,
+                         const double *hgrids, double eta, const double *dlogeps, double *rhopol,
+                         double *rhores2);
+int oracle_div_u_i_ref(int geocode, int n01, int n02, int n03, const double *u, double *du,
+                       int nord, const double *hgrids);
 int oracle_hamiltonian(const int *n, const int *bc, const double *a_kin, const double *psig,
                        const double *pot, double *rho, double *hpsig, double *ekin, double *epot);
 

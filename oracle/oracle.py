@@ -48,6 +48,14 @@ _SIGS['oracle_d_kin'] = [_int, _I, _I, _D, _D, _D, _D, _D, _dbl, _dbl]
 _SIGS['oracle_d_dwt_sym8'] = [_int, _I, _I, _D, _D, _D, _D]
 _SIGS['oracle_d_idwt_sym8'] = _SIGS['oracle_d_dwt_sym8']
 _SIGS['oracle_hamiltonian'] = [_I, _I, _D, _D, _D, _D, _D, _D, _D]
+_SIGS['oracle_poisson_broker'] = [_int, _int, _I, _int, _D, _D, _dbl]
+_SIGS['oracle_div_u_i'] = [_int, _int, _int, _int, _D, _D, _int, _D, _D]
+_SIGS['oracle_nabla_u'] = [_int, _int, _int, _int, _D, _D, _int, _D]
+_SIGS['oracle_nabla_u_and_square'] = [_int, _int, _int, _int, _D, _D, _D, _int, _D]
+_SIGS['oracle_nabla_u_square'] = [_int, _int, _int, _int, _D, _D, _int, _D]
+_SIGS['oracle_nabla_u_epsilon'] = [_int, _int, _int, _int, _D, _D, _int, _D, _D]
+_SIGS['oracle_update_rhopol'] = [_int, _int, _int, _int, _D, _int, _D, _dbl, _D, _D, _D]
+_SIGS['oracle_div_u_i_ref'] = [_int, _int, _int, _int, _D, _D, _int, _D]
 
 
 def build(ref=None):
@@ -72,7 +80,7 @@ def lib():
         for name, args in _SIGS.items():
             fn = getattr(L, name)
             fn.argtypes = args
-            fn.restype = ctypes.c_int if name.startswith(('oracle_d_', 'oracle_hamiltonian')) else None
+            fn.restype = None if name.endswith(('_per_ref', '_per_t_ref', '_free_ref', '_free_t_ref', '_ref_ekin')) or name == 'oracle_kinetic_per_ref' else ctypes.c_int
         _LIB = L
     return _LIB
 
