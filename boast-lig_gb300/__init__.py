@@ -428,6 +428,87 @@ class Fortran:
         return out[0] if work else list(out)
 
 
+# ---- Poisson finite-difference operators (BigDFT/Poisson.rb) ----------------------
+BC_NPERIODIC = -2
+
+
+class Poisson:
+    """Host-array calls of the Poisson operators (Poisson_broker, div_u_i,
+    nabla_u, nabla_u_and_square, nabla_u_square, nabla_u_epsilon,
+    update_rhopol); arrays are float64, Fortran order, flat."""
+
+    _SIG = {
+        'Poisson_broker': [_int, _int, _I, _int, _vp, _vp, _dbl],
+        'div_u_i': [_int, _int, _int, _int, _vp, _vp, _int, _D, _vp],
+        'nabla_u': [_int, _int, _int, _int, _vp, _vp, _int, _D],
+        'nabla_u_and_square': [_int, _int, _int, _int, _vp, _vp, _vp, _int, _D],
+        'nabla_u_square': [_int, _int, _int, _int, _vp, _vp, _int, _D],
+        'nabla_u_epsilon': [_int, _int, _int, _int, _vp, _vp, _int, _D, _vp],
+        'update_rhopol': [_int, _int, _int, _int, _vp, _int, _D, _dbl, _vp, _vp, _vp],
+    }
+
+    def __init__(self):
+        L = lib()
+        for name, args in self._SIG.items():
+            getattr(L, name).argtypes = args
+            getattr(L, name).restype = _int
+        self.L = L
+
+    def _call(self, name, *args):
+        conv = []
+        for a, t in zip(args, self._SIG[name]):
+            if t is _I:
+                conv.append(_ints(a))
+            elif t is _D:
+                conv.append(_dbls(a))
+            elif t is _vp:
+                conv.append(_host_ptr(a, True) if a is not None else None)
+            else:
+                conv.append(a)
+        st = getattr(self.L, name)(*conv)
+        if st:
+            raise LibconvError(st, name, last_error())
+
+    def broker(self, nord, idim, nn, bc, u, a):
+        du = np.zeros(int(np.prod(nn)))
+        self._call('Poisson_broker', nord, idim, nn, bc, u, du, float(a))
+        return du
+
+    def div_u_i(self, geocode, n, u, nord, h, cc=False):
+        N = int(np.prod(n))
+        du = np.zeros(N)
+        c = np.zeros(N) if cc else None
+        self._call('div_u_i', geocode, *n, u, du, nord, h, c)
+        return (du, c) if cc else du
+
+    def nabla_u(self, geocode, n, u, nord, h):
+        du = np.zeros(3 * int(np.prod(n)))
+        self._call('nabla_u', geocode, *n, u, du, nord, h)
+        return du
+
+    def nabla_u_and_square(self, geocode, n, u, nord, h):
+        N = int(np.prod(n))
+        du, ddu = np.zeros(3 * N), np.zeros(N)
+        self._call('nabla_u_and_square', geocode, *n, u, du, ddu, nord, h)
+        return du, ddu
+
+    def nabla_u_square(self, geocode, n, u, nord, h):
+        ddu = np.zeros(int(np.prod(n)))
+        self._call('nabla_u_square', geocode, *n, u, ddu, nord, h)
+        return ddu
+
+    def nabla_u_epsilon(self, geocode, n, u, nord, h, eps):
+        du = np.zeros(3 * int(np.prod(n)))
+        self._call('nabla_u_epsilon', geocode, *n, u, du, nord, h, eps)
+        return du
+
+    def update_rhopol(self, geocode, n, u, nord, h, eta, dlogeps, rhopol):
+        """rhopol is updated in place; returns rhores2."""
+        r2 = np.zeros(1)
+        self._call('update_rhopol', geocode, *n, u, nord, h, float(eta), dlogeps, rhopol, r2)
+        return float(r2[0])
+
+
 # ---- batched operators over many uneven grids ------------------------------------
 BATCH_OP_MF, BATCH_OP_KIN = 0, 1
 ENGINE_FP64_Q64, ENGINE_FP64_Q32, ENGINE_TC = 0, 1, 2

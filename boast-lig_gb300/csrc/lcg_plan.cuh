@@ -2,6 +2,7 @@
 // (x, y, w1, w2) each sweep reads and writes.  Shared by the C-ABI entry
 // points and the batched (many-grid) operators.
 #pragma once
+#include <mutex>
 #include <vector>
 
 #include "lcg_sweep.cuh"
@@ -51,6 +52,15 @@ int sum1d_generic(int op_id, int d, const int *n, const int *bc, const int *nx, 
 // Per-axis input/output extents of op_id's sweeps and the largest
 // intermediate (elements) of the multi-D product; any output may be null.
 int extents(int op_id, int d, const int *n, const int *bc, int *in, int *out, long long *inter);
+// One Poisson finite-difference sweep on device pointers (bc 0 periodic or
+// LIBCONV_BC_NPERIODIC), y = a d/dx_idim x, or y += ... when accumulate.
+int poisson_sweep(int nord, int idim, const int *nn, int bc, double a, bool accumulate,
+                  const double *x, double *y, cudaStream_t st);
+// Host-pointer composition: hold library_lock(), stage in host_staging(),
+// run on its stream, then host_finish() (synchronise + device status).
+std::unique_lock<std::recursive_mutex> library_lock();
+double *host_staging(size_t bytes, cudaStream_t &st, int &rc);
+int host_finish(cudaStream_t st);
 int report(int code, const char *msg);
 int report_cuda(cudaError_t e, const char *what);
 

@@ -53,6 +53,11 @@ cudaError_t launch_dot_reduce(const double *part, long long count, double *out, 
 // for j < nseg (fixed order), on `st`.
 cudaError_t launch_dot_reduce_seg(const double *part, long long seg_len, int nseg, double *out,
                                   long long out_stride, cudaStream_t st);
+// The m = nord/2 one-sided outputs at each end of every line of a
+// non-periodic Poisson sweep (c1D(:, i-m) on the first nord+1 points, c1D(:,
+// i-n+m+1) on the last), y = a * sum (or y += when accumulate).
+cudaError_t launch_poisson_edges(const double *x, double *y, long long nL, int n, long long nR,
+                                 int nord, double a, int accumulate, cudaStream_t st);
 // Potential step of the local Hamiltonian over norb orbitals of `count`
 // real-space points each (psir back to back): rho += sum_j psir_j^2 (rho may
 // be null), epot[j * epot_stride] = sum pot psir_j^2, psir_j = pot psir_j.

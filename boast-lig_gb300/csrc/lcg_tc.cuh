@@ -49,6 +49,10 @@ cudaError_t launch_sweep_tc_batch(int kind, int ntaps, const Sweep *descs, const
 
 namespace tck {
 long long tile_count_for(const Sweep &S, int qp);
+// 17-tap convolution (the Poisson finite differences), every scheme; its own
+// translation unit.
+cudaError_t launch_fd(const Sweep &S, const TcFilter &F, int sch, int *status, const int *lineE,
+                      cudaStream_t st);
 int sm_count();
 // Per-scheme launchers (one translation unit each).
 cudaError_t launch_exact(const Sweep &S, const TcFilter &F, int *status, const int *lineE,

@@ -120,9 +120,10 @@ struct DevState {
     DevBuf status;                   // device status word (bounded waits)
     DevBuf potpart;                  // partial sums of the potential energy
     DevBuf hbuf;                     // staging of the host-pointer local Hamiltonian
+    DevBuf pbuf;                     // staging of the host-pointer Poisson operators
 };
 
-std::mutex g_mu;
+std::recursive_mutex g_mu;   // recursive: composed host entry points hold it across sweeps
 DevState g_dev[64];
 
 int current_device(int &dev) {
@@ -433,7 +434,7 @@ int exec_dev(const Plan &P, const double *x, double *y, double *w1, double *w2, 
     if (P.elems[B_W2] && !w2) return fail(LIBCONV_EARG, "w2 workspace required");
     if (P.has_dot && !dot_dev) return fail(LIBCONV_EARG, "dot_in must not be null");
     double *bufs[4] = {const_cast<double *>(x), y, w1, w2};
-    std::lock_guard<std::mutex> lk(g_mu);
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
     int rc;
     DevState *s = dev_state(rc);
     if (!s) return rc;
@@ -456,7 +457,7 @@ int read_status(DevState &s) {
 int exec_host(const Plan &P, const double *x, double *y, double *dot_host) {
     if (!x || !y) return fail(LIBCONV_EARG, "x/y must not be null");
     if (P.has_dot && !dot_host) return fail(LIBCONV_EARG, "dot_in must not be null");
-    std::lock_guard<std::mutex> lk(g_mu);
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
     int rc;
     DevState *s = dev_state(rc);
     if (!s) return rc;
@@ -572,7 +573,7 @@ int ham_host(const Ham &H, const double *psig, const double *pot, double *rho, d
              double *energies) {
     if (!psig || !pot || !hpsig || !energies)
         return fail(LIBCONV_EARG, "psig/pot/hpsig/energies must not be null");
-    std::lock_guard<std::mutex> lk(g_mu);
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
     int rc;
     DevState *s = dev_state(rc);
     if (!s) return rc;
@@ -752,6 +753,86 @@ int extents(int op_id, int d, const int *n, const int *bc, int *in, int *out, lo
     return LIBCONV_OK;
 }
 
+// One Poisson broker sweep (Poisson.rb:1951-2043 over the generated 1D
+// operator with the PoissonFilter, GenericConvolution2.rb:237-294) on device
+// pointers: y = a d/dx_idim x (accumulate: y += ...).  The central stencil
+// (17 taps, zero padded below nord 16) runs as a convolution sweep: periodic,
+// or, for the non-periodic boundary, only over the outputs m..n-m-1 whose
+// stencil stays inside the line; the m one-sided outputs at each end are
+// written by launch_poisson_edges.
+int poisson_sweep(int nord, int idim, const int *nn, int bc, double a, bool accumulate,
+                  const double *x, double *y, cudaStream_t st) {
+    int ftab;
+    switch (nord) {
+    case 2: ftab = LCG_FTAB_FD2; break;
+    case 4: ftab = LCG_FTAB_FD4; break;
+    case 6: ftab = LCG_FTAB_FD6; break;
+    case 8: ftab = LCG_FTAB_FD8; break;
+    case 16: ftab = LCG_FTAB_FD16; break;
+    default: return fail(LIBCONV_EARG, "nord=%d: only 2, 4, 6, 8 and 16", nord);
+    }
+    if (!nn || !x || !y) return fail(LIBCONV_EARG, "nn/u/du must not be null");
+    if (idim < 0 || idim > 2) return fail(LIBCONV_EARG, "idim=%d out of [0,2]", idim);
+    if (bc != BC_PERIODIC && bc != LIBCONV_BC_NPERIODIC)
+        return fail(LIBCONV_EBC, "Poisson operators take periodic (0) or non-periodic (-2), bc=%d", bc);
+    for (int i = 0; i < 3; ++i)
+        if (nn[i] < 1) return fail(LIBCONV_EARG, "nn[%d]=%d", i, nn[i]);
+    const int n = nn[idim], m = nord / 2;
+    const bool nper = bc == LIBCONV_BC_NPERIODIC;
+    if (nper && n < nord + 1)
+        return fail(LIBCONV_ESIZE, "non-periodic axis of %d points shorter than the %d-point stencil",
+                    n, nord + 1);
+    long long nL = 1, nR = 1;
+    for (int i = 0; i < idim; ++i) nL *= nn[i];
+    for (int i = idim + 1; i < 3; ++i) nR *= nn[i];
+    if (nL * nR > (1LL << 31) - 1 || nL * nR * n > (1LL << 40)) return fail(LIBCONV_EARG, "grid too large");
+    const OpDef fd = {KCONV, {ftab, ftab}, {LCG_FD_NTAPS, LCG_FD_NTAPS}, {LCG_FD_LOWFIL, LCG_FD_LOWFIL},
+                      LCG_FD_NTAPS, 2 * LCG_FD_NTAPS};
+    Plan P;
+    PlanStep ps;
+    geometry(fd, nper ? BC_FREE : BC_PERIODIC, (int)nL, n, (int)nR, n, n, ps.S);
+    ps.S.has_a = 1;
+    ps.S.a = a;
+    ps.S.ay_mode = accumulate ? 2 : 0;
+    if (nper) { ps.S.qlo = m; ps.S.qhi = n - m - 1; }
+    ps.S.x_arr = ps.S.y_arr = nL * n * nR;
+    ps.src = B_X; ps.dst = B_Y; ps.src2 = -1;
+    P.steps.push_back(ps);
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    int rc;
+    DevState *s = dev_state(rc);
+    if (!s) return rc;
+    double *bufs[4] = {const_cast<double *>(x), y, nullptr, nullptr};
+    if ((rc = run_plan(P, bufs, s->scratch, s->lineexp, nullptr, (int *)s->status.p, st))) return rc;
+    if (nper) {
+        cudaError_t e = launch_poisson_edges(x, y, nL, n, nR, nord, a, accumulate ? 1 : 0, st);
+        if (e != cudaSuccess) return cuda_fail(e, "Poisson boundary launch");
+    }
+    return LIBCONV_OK;
+}
+
+// Device staging for composed host-pointer entry points: `bytes` of the
+// library's buffer and its stream.  The caller holds library_lock().
+double *host_staging(size_t bytes, cudaStream_t &st, int &rc) {
+    DevState *s = dev_state(rc);
+    if (!s) return nullptr;
+    if ((rc = ensure(s->pbuf, bytes))) return nullptr;
+    st = s->stream;
+    return (double *)s->pbuf.p;
+}
+std::unique_lock<std::recursive_mutex> library_lock() {
+    return std::unique_lock<std::recursive_mutex>(g_mu);
+}
+// Synchronise the library stream and read the device status word.
+int host_finish(cudaStream_t st) {
+    int rc;
+    DevState *s = dev_state(rc);
+    if (!s) return rc;
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "synchronize");
+    return read_status(*s);
+}
+
 int report(int code, const char *msg) { return fail(code, "%s", msg); }
 int report_cuda(cudaError_t e, const char *what) { return cuda_fail(e, what); }
 
@@ -766,7 +847,7 @@ int plan_kinetic(int d, const int *n, const int *bc, const double *a, double a_x
 const double *filter_table() { return h_ftab; }
 int current_mode() { return t_mode; }
 int *device_status(int &rc) {
-    std::lock_guard<std::mutex> lk(g_mu);
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
     DevState *s = dev_state(rc);
     return s ? (int *)s->status.p : nullptr;
 }
@@ -795,7 +876,7 @@ const char *libconv_gb300_strerror(int s) {
 const char *libconv_gb300_last_error(void) { return t_err.c_str(); }
 
 int libconv_gb300_check(void *stream) {
-    std::lock_guard<std::mutex> lk(g_mu);
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
     int rc;
     DevState *s = dev_state(rc);
     if (!s) return rc;
@@ -1031,7 +1112,7 @@ int libconv_hamiltonian_narr_dev(const int *n, const int *bc, const double *a_ki
     Ham H;
     int rc = plan_ham(n, bc, a_kin, norb, H);
     if (rc) return rc;
-    std::lock_guard<std::mutex> lk(g_mu);
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
     DevState *s = dev_state(rc);
     if (!s) return rc;
     return run_ham(H, psig, pot, rho, hpsig, work, energies, *s, (cudaStream_t)stream);

@@ -291,6 +291,7 @@ long long sweep_fp64_blocks(const Sweep &S) {
 
 cudaError_t launch_sweep_fp64(const Sweep &S, cudaStream_t st) {
     if (S.kind == KCONV && S.ntaps == 16) return launch_t<KCONV, 16>(S, st);
+    if (S.kind == KCONV && S.ntaps == 17) return launch_t<KCONV, 17>(S, st);
     if (S.kind == KCONV && S.ntaps == 29) return launch_t<KCONV, 29>(S, st);
     if (S.kind == KDEC && S.ntaps == 8) return launch_t<KDEC, 8>(S, st);
     if (S.kind == KDEC && S.ntaps == 16) return launch_t<KDEC, 16>(S, st);

@@ -77,7 +77,7 @@ __global__ void line_exp_kernel(const Sweep S, int plen, int *out) {
 long long sweep_tc_lines(const Sweep &S) { return (long long)S.nL * S.nR * S.narr; }
 
 bool sweep_tc_supported(const Sweep &S) {
-    if (S.kind == KCONV) return S.ntaps == 16 || S.ntaps == 29;
+    if (S.kind == KCONV) return S.ntaps == 16 || S.ntaps == 17 || S.ntaps == 29;
     return (S.kind == KDEC || S.kind == KREC) && (S.ntaps == 8 || S.ntaps == 16);
 }
 

@@ -9,6 +9,7 @@ namespace tck {
 cudaError_t launch_tf32x3(const Sweep &S, const TcFilter &F, int *status, const int *lineE,
                           cudaStream_t st) {
     if (S.kind == KCONV && S.ntaps == 16) return launch<KCONV, 16, SCH_TF32X3>(S, F, status, lineE, st);
+    if (S.kind == KCONV && S.ntaps == 17) return launch_fd(S, F, SCH_TF32X3, status, lineE, st);
     if (S.kind == KCONV && S.ntaps == 29) return launch<KCONV, 29, SCH_TF32X3>(S, F, status, lineE, st);
     if (S.kind == KDEC && S.ntaps == 8) return launch<KDEC, 8, SCH_TF32X3>(S, F, status, lineE, st);
     if (S.kind == KDEC && S.ntaps == 16) return launch<KDEC, 16, SCH_TF32X3>(S, F, status, lineE, st);

@@ -45,6 +45,7 @@ extern "C" {
 #define LIBCONV_BC_PERIODIC  0
 #define LIBCONV_BC_GROW      1
 #define LIBCONV_BC_FREE      2
+#define LIBCONV_BC_NPERIODIC -2   /* non-periodic: one-sided stencils (Poisson operators) */
 
 /* Compute modes for libconv_gb300_set_mode (per calling thread).  The
  * tensor-core modes cover every sweep (MagicFilter, kinetic, derivative,
@@ -284,6 +285,65 @@ int libconv_hamiltonian_narr(const int *n, const int *bc, const double *a_kin, i
 int libconv_hamiltonian_narr_dev(const int *n, const int *bc, const double *a_kin, int norb,
                                  const double *psig, const double *pot, double *rho,
                                  double *hpsig, double *energies, double *work, void *stream);
+
+/* ---------------------------------------------------------------------
+ * Poisson finite-difference operators (BigDFT/Poisson.rb): first
+ * derivatives of order nord in {2, 4, 6, 8, 16} (the c1D table of
+ * Poisson.rb:20-166), periodic or non-periodic (LIBCONV_BC_NPERIODIC:
+ * one-sided stencils on the nord/2 first and last points of a line, which
+ * needs at least nord + 1 points).  Grids are n01 x n02 x n03, Fortran
+ * order; hgrids[3] (host) are the spacings, each derivative scaled by
+ * 1/hgrids[i] as the generated drivers do.  geocode selects the axes:
+ * 1 free (x, z non-periodic), 2 periodic, 3 surface (y non-periodic)
+ * (Poisson.rb:2122-2128).  The calling thread's compute mode applies.
+ * ------------------------------------------------------------------- */
+/* Poisson_broker (Poisson.rb:1951-2043): du = a d/dx_idim u on the 3D grid
+ * nn[3], idim 0..2, bc LIBCONV_BC_PERIODIC or LIBCONV_BC_NPERIODIC. */
+int Poisson_broker(int nord, int idim, const int *nn, int bc, const double *u, double *du,
+                   double a);
+int Poisson_broker_dev(int nord, int idim, const int *nn, int bc, const double *u, double *du,
+                       double a, void *stream);
+/* div_u_i (Poisson.rb:2067-2194): u(n01,n02,n03,3) -> du = sum_i d_i u_i;
+ * when cc is not NULL also cc = sum_i u_i^2 d_i u_i
+ * + 2 (u0 u1 d0 u1 + u0 u2 d0 u2 + u1 u2 d1 u2).  _dev: work of
+ * 5 n01 n02 n03 doubles when cc is given (unused otherwise). */
+int div_u_i(int geocode, int n01, int n02, int n03, const double *u, double *du, int nord,
+            const double *hgrids, double *cc);
+int div_u_i_dev(int geocode, int n01, int n02, int n03, const double *u, double *du, int nord,
+                const double *hgrids, double *cc, double *work, void *stream);
+/* nabla_u (Poisson.rb:2553-2620): du(n01,n02,n03,3) = grad u. */
+int nabla_u(int geocode, int n01, int n02, int n03, const double *u, double *du, int nord,
+            const double *hgrids);
+int nabla_u_dev(int geocode, int n01, int n02, int n03, const double *u, double *du, int nord,
+                const double *hgrids, void *stream);
+/* nabla_u_and_square (Poisson.rb:2197-2275): du = grad u, ddu = |grad u|^2. */
+int nabla_u_and_square(int geocode, int n01, int n02, int n03, const double *u, double *du,
+                       double *ddu, int nord, const double *hgrids);
+int nabla_u_and_square_dev(int geocode, int n01, int n02, int n03, const double *u, double *du,
+                           double *ddu, int nord, const double *hgrids, void *stream);
+/* nabla_u_square (Poisson.rb:2278-2359): ddu = |grad u|^2.  _dev: work of
+ * 3 n01 n02 n03 doubles. */
+int nabla_u_square(int geocode, int n01, int n02, int n03, const double *u, double *ddu, int nord,
+                   const double *hgrids);
+int nabla_u_square_dev(int geocode, int n01, int n02, int n03, const double *u, double *ddu,
+                       int nord, const double *hgrids, double *work, void *stream);
+/* nabla_u_epsilon (Poisson.rb:2362-2443): du = eps grad u. */
+int nabla_u_epsilon(int geocode, int n01, int n02, int n03, const double *u, double *du, int nord,
+                    const double *hgrids, const double *eps);
+int nabla_u_epsilon_dev(int geocode, int n01, int n02, int n03, const double *u, double *du,
+                        int nord, const double *hgrids, const double *eps, void *stream);
+/* update_rhopol (Poisson.rb:2446-2550): res = (dlogeps . grad u)/(4 pi),
+ * res = eta (res - rhopol), rhopol += res, *rhores2 = sum res^2;
+ * dlogeps(3,n01,n02,n03) component fastest.  _dev: rhores2 is a device
+ * pointer, work of update_rhopol_work_size doubles. */
+int update_rhopol(int geocode, int n01, int n02, int n03, const double *u, int nord,
+                  const double *hgrids, double eta, const double *dlogeps, double *rhopol,
+                  double *rhores2);
+int update_rhopol_dev(int geocode, int n01, int n02, int n03, const double *u, int nord,
+                      const double *hgrids, double eta, const double *dlogeps, double *rhopol,
+                      double *rhores2, double *work, void *stream);
+/* Extension: work size (doubles) of update_rhopol_dev. */
+int update_rhopol_work_size(int n01, int n02, int n03, long long *nwork);
 
 /* ---------------------------------------------------------------------
  * Cost model (ConvolutionOperator1d#cost / GenericConvolutionOperator#cost,
