@@ -15,7 +15,7 @@ uniform [-1, 1], details uniform [-1, 1] x 1e-3) into 96^3, then analysis
 back; metric: 96^3 grid points per second through both transforms.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload mfkin128|wavelet96|orbitals512|precond256|hamiltonian48]
+                  [--workload mfkin128|wavelet96|orbitals512|precond256|hamiltonian48|poisson256]
                   [--mode tc_exact|fp64|tc_bf16x3|tc_tf32x3]
 
 Workload orbitals512: 512 orbitals with axes uniform in {24..72} (seed 7),
@@ -33,6 +33,9 @@ Workload hamiltonian48: the local Hamiltonian of orbitals on a 48^3 coarse
 grid with free boundaries (libconv_hamiltonian_dev: idwt grow, MagicFilter
 grow, potential and density, inverse MagicFilter shrink, kinetic with the
 energies, dwt shrink), 32 orbitals per step; metric: orbitals/s.
+
+Workload poisson256: the Poisson test's div_u_i with cc on 256^3 (nord 16,
+geocode 3, h = 0.1, u uniform [0, 1)); metric: grid points per second.
 
 Modes: tc_exact (default) runs the tensor-core exact-digit sweeps (FP64
 accuracy); fp64 the FP64 FMA sweeps; tc_bf16x3 / tc_tf32x3 the split-precision
@@ -273,6 +276,21 @@ class Hamiltonian48:
         O.call('oracle_hamiltonian', self.n, self.bc, np.array(self.a), x, pot, None, hpsig, ek, ep)
 
 
+class Poisson256:
+    """div_u_i with cc on the Poisson test's 256^3 grid (Poisson_test.rb:5-19)."""
+    name = 'poisson256'
+    metric = ('grid pts/s, Poisson div_u_i with cc (16th-order finite differences, 256^3, '
+              'geocode 3: y non-periodic, h = 0.1)')
+    n = [256, 256, 256]
+    geocode = 3
+    nord = 16
+    h = [0.1, 0.1, 0.1]
+    # per point: six derivative sweeps (read 8, write 8 B) and the cc kernel
+    # (read u 24, du 8, five derivatives 40; write cc 8, du 8)
+    bytes_per_pt = 6 * 16 + 88
+    sweep_bytes_per_pt = 16
+
+
 def cpu_cg(O, n, h, eps, b, tol, maxit=3000):
     """Plain (Jacobi) CG on the host with the oracle's kinetic operator; returns
     the iteration count."""
@@ -323,7 +341,8 @@ def cpu_solves(W, seconds):
 
 
 WORKLOADS = {'mfkin128': MfKin128(), 'wavelet96': Wavelet96(), 'orbitals512': Orbitals512(),
-             'precond256': Precond256(), 'hamiltonian48': Hamiltonian48()}
+             'precond256': Precond256(), 'hamiltonian48': Hamiltonian48(),
+             'poisson256': Poisson256()}
 
 
 class Clocks:
@@ -531,11 +550,63 @@ def run_reference_hamiltonian(args, W):
     print(json.dumps(line), flush=True)
 
 
+def cpu_poisson(W, seconds, n=(128, 128, 128)):
+    """oracle_div_u_i with cc on one 128^3 grid per host thread, repeated for
+    about `seconds`; returns (points, time, threads)."""
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    O.lib()
+    th = cpu_threads()
+    N = int(np.prod(n))
+    rng = np.random.default_rng(5)
+    us = [rng.uniform(0, 1, 3 * N) for _ in range(2)]
+    bufs = [(np.zeros(N), np.zeros(N)) for _ in range(th)]
+    done = [0] * th
+    h = np.array(W.h)
+    t0 = time.perf_counter()
+
+    def work(t):
+        while True:
+            du, cc = bufs[t]
+            O.call('oracle_div_u_i', W.geocode, *n, us[t % 2], du, W.nord, h, cc)
+            done[t] += N
+            if time.perf_counter() - t0 >= seconds:
+                break
+
+    ts = [threading.Thread(target=work, args=(t,)) for t in range(th)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    return sum(done), time.perf_counter() - t0, th
+
+
+def run_reference_poisson(args, W):
+    vals = []
+    for _ in range(max(args.steps, 1)):
+        pts, t, th = cpu_poisson(W, 10.0)
+        vals.append(pts / t)
+    v = float(np.median(vals))
+    line = {'impl': 'reference', 'metric': W.metric, 'value': v, 'unit': UNIT,
+            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': int(np.prod(W.n)) / v * 1e3, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic (seeded)',
+            'config': {'workload': f'oracle_div_u_i with cc (C restatement of the generated '
+                                   f'driver), one 128^3 grid per host thread, {th} threads, '
+                                   '~10 s per step', 'grid': [128, 128, 128]},
+            'cpu_baseline': {'value': v, 'unit': UNIT, 'cores': th, 'kind': 'port',
+                             'sample': '128^3 grids processed in ~10 s per step'},
+            'e2e': {'value': v, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get('RANK', '0'))
     if rank != 0:
         return
     W = WORKLOADS[args.workload]
+    if W.name == 'poisson256':
+        return run_reference_poisson(args, W)
     if W.name == 'hamiltonian48':
         return run_reference_hamiltonian(args, W)
     if W.name == 'orbitals512':
@@ -1027,10 +1098,158 @@ def run_hamiltonian(args, W):
         dist.destroy_process_group()
 
 
+def run_poisson(args, W):
+    """div_u_i with cc on one 256^3 field per GPU per step (device pointers,
+    one stream), timed with CUDA events; e2e through the host-pointer call."""
+    import ctypes
+    import torch
+    pkg = package()
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl', device_id=dev)
+    pkg.set_mode(getattr(pkg, MODES[args.mode]))
+    n = W.n
+    N = int(np.prod(n))
+    gen = torch.Generator().manual_seed(256 + rank)
+    host_u = torch.rand(3 * N, generator=gen, dtype=torch.float64).pin_memory()
+    du_ = host_u.to(dev)
+    ddu = torch.empty(N, dtype=torch.float64, device=dev)
+    dcc = torch.empty(N, dtype=torch.float64, device=dev)
+    work = torch.empty(5 * N, dtype=torch.float64, device=dev)
+    L = pkg.lib()
+    f = L.div_u_i_dev
+    f.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_double)] + [ctypes.c_void_p] * 3
+    f.restype = ctypes.c_int
+    h = (ctypes.c_double * 3)(*W.h)
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def step():
+        st = f(W.geocode, *n, du_.data_ptr(), ddu.data_ptr(), W.nord, h, dcc.data_ptr(),
+               work.data_ptr(), sp)
+        if st:
+            raise pkg.LibconvError(st, 'div_u_i_dev', pkg.last_error())
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    stream.synchronize()
+    pkg.check(stream)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    clocks = Clocks(local)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    start.record(stream)
+    for _ in range(args.steps):
+        step()
+    stop.record(stream)
+    stop.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    ck = clocks.stop()
+    pkg.check(stream)
+    ms = start.elapsed_time(stop)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = t.item()
+    value = N * world * args.steps / (ms / 1e3)
+
+    # one derivative sweep timed alone (the dominant kernel): d/dz of u0
+    fb = L.Poisson_broker_dev
+    fb.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p]
+    fb.restype = ctypes.c_int
+    nn = (ctypes.c_int * 3)(*n)
+    reps = 10
+    for _ in range(3):
+        fb(W.nord, 2, nn, 0, du_.data_ptr(), ddu.data_ptr(), 10.0, sp)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fb(W.nord, 2, nn, 0, du_.data_ptr(), ddu.data_ptr(), 10.0, sp)
+    e1.record(stream)
+    e1.synchronize()
+    t_sweep = e0.elapsed_time(e1) / reps / 1e3
+
+    # e2e: the host-pointer div_u_i with cc (H2D of u, D2H of du and cc)
+    hu = host_u.numpy()
+    hdu = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    hcc = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    fh = L.div_u_i
+    fh.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]
+    fh.restype = ctypes.c_int
+
+    def host_step():
+        st = fh(W.geocode, *n, hu.ctypes.data, hdu.ctypes.data, W.nord, h, hcc.ctypes.data)
+        if st:
+            raise pkg.LibconvError(st, 'div_u_i', pkg.last_error())
+
+    host_step()
+    barrier()
+    e_steps = max(2, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e_steps):
+        host_step()
+    barrier()
+    e_t = (time.perf_counter() - t0) / e_steps
+    e2e = {'value': N * world / e_t, 'unit': UNIT, 'h2d_bytes_per_step': 3 * N * 8,
+           'd2h_bytes_per_step': 2 * N * 8, 'note': 'div_u_i (host pointers) with cc'}
+    pk = peaks()
+    achieved = W.sweep_bytes_per_pt * N / t_sweep / 1e9
+    step_s = ms / 1e3 / args.steps
+    roof = {'bound': 'hbm', 'achieved': achieved, 'peak': pk['hbm'], 'unit': 'GB/s',
+            'frac': achieved / pk['hbm'], 'traffic': None, 'peak_source': pk['source'],
+            'kernel': f'one periodic 17-tap derivative sweep along z ({args.mode}), timed alone',
+            'algorithmic_bytes_per_point': W.sweep_bytes_per_pt,
+            'step': {'algorithmic_bytes_per_point': W.bytes_per_pt,
+                     'achieved_gbs': W.bytes_per_pt * N / step_s / 1e9,
+                     'frac': W.bytes_per_pt * N / step_s / 1e9 / pk['hbm']}}
+    launches = {'tc_exact': 15, 'fp64': 9}.get(args.mode, 9)
+    exact = args.mode in ('fp64', 'tc_exact')
+    line = {'metric': W.metric, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+            'warmup': max(args.warmup, 3), 'ms_per_step': ms / args.steps,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f64' if exact else ('f64 in HBM, ' + args.mode[3:] + ' split on tensor cores'),
+            'data': 'synthetic (seeded uniform [0,1), as the reference test)',
+            'config': {'workload': 'div_u_i_dev with cc, 256^3, nord 16, geocode 3, h 0.1: six '
+                                   'derivative sweeps and the cc kernel per step',
+                       'mode': args.mode, 'grid': n,
+                       'l2': f'inputs larger than L2 ({3 * N * 8 / 1e6:.0f} MB of u)',
+                       'ms_sweep': t_sweep * 1e3},
+            'clocks': ck, 'e2e': e2e, 'gpu_launches': args.steps * launches, 'roofline': roof}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        pts, t, th = cpu_poisson(W, 10.0)
+        line['cpu_baseline'] = {'value': pts / t, 'unit': UNIT, 'cores': th, 'kind': 'port',
+                                'sample': f'{pts // (128 ** 3)} grids of 128^3 in {t:.1f} s, '
+                                          'oracle_div_u_i with cc, one grid per host thread'}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
 def run_gpu(args):
     import torch
     pkg = package()
     W = WORKLOADS[args.workload]
+    if W.name == 'poisson256':
+        return run_poisson(args, W)
     if W.name == 'hamiltonian48':
         return run_hamiltonian(args, W)
     if W.name == 'orbitals512':
