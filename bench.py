@@ -86,6 +86,9 @@ class MfKin128:
     ops = ('magicfilter3d', 'kinetic3d')
     a = [-0.5 / HGRID ** 2] * 3
     launches = 6                                     # 3 sweeps per operator
+    # exact tensor-core mode: a line-exponent pass before each MagicFilter sweep, one shared
+    # pass over x for the three kinetic sweeps
+    exact_prepasses = 4
     desc = ('{B} grids of 128^3 periodic per GPU per step: MagicFilter3D (d_sfrf_ld_narr) + '
             'Kinetic3D (d_kin_narr, h=0.45)')
 
@@ -145,6 +148,7 @@ class Wavelet96:
     n_out = 96 ** 3
     ops = ('idwt3d', 'dwt3d')
     launches = 6
+    exact_prepasses = 6                              # one line-exponent pass per sweep
     desc = ('{B} grids per GPU per step: d_idwt_sym8_narr (8 subbands of 48^3 -> 96^3) then '
             'd_dwt_sym8_narr (96^3 -> 8 x 48^3)')
 
@@ -1395,8 +1399,9 @@ def run_gpu(args):
                        'l2': f'inputs larger than L2 ({B * Ni * 8 / 1e6:.0f} MB per array)',
                        **{f'ms_{o}': t / args.steps for o, t in zip(W.ops, op_ms)}},
             'clocks': ck, 'e2e': e2e,
-            # each exact tensor-core sweep is preceded by its line-exponent pass
-            'gpu_launches': args.steps * W.launches * (2 if args.mode == 'tc_exact' else 1),
+            # exact tensor-core sweeps are preceded by line-exponent passes
+            'gpu_launches': args.steps * (W.launches + (W.exact_prepasses if args.mode == 'tc_exact'
+                                                        else 0)),
             'roofline': roof}
     if accuracy:
         line['accuracy_max_rel_error'] = accuracy

@@ -333,10 +333,10 @@ class Hamiltonian:
         self.work = torch.empty(nwork, dtype=torch.float64, device=device)
         self.energies = torch.zeros(self.norb, 4, dtype=torch.float64, device=device)
 
-    # kernel launches of one call: 15 sweeps (x2 in the exact tensor-core mode,
-    # whose sweeps each follow a line-exponent pass), the potential kernel and
-    # its reduction, and the three kinetic-energy reductions
-    LAUNCHES = {'exact': 35, 'other': 20}
+    # kernel launches of one call: 15 sweeps, in the exact tensor-core mode 13
+    # line-exponent passes (one shared by the three kinetic sweeps), the
+    # potential kernel and its reduction, and the three kinetic-energy reductions
+    LAUNCHES = {'exact': 33, 'other': 20}
 
     def __call__(self, psig, pot, hpsig, rho=None, stream=None, energies=None):
         """energies: optional device tensor of norb * 4 doubles to receive the

@@ -16,6 +16,7 @@ struct PlanStep {
     int src, dst, src2;   // buffer ids (src2 = -1 if no x2)
     int dot_slot = 0;     // entry of the dot output this step's dot product goes to
     int dot_stride = 0;   // > 0: one dot per array, array j at dot_slot + j * dot_stride
+    int exp_axis = -1;    // >= 0: line exponents from the plan's shared pass over x (this axis)
 };
 
 struct Plan {
@@ -24,6 +25,8 @@ struct Plan {
     size_t y_read = 0;                // y is read (a_y != 0)
     int has_dot = 0;
     int ndot = 1;                     // dot outputs (one per kinetic direction for ekin)
+    int exp3[4] = {0, 0, 0, 0};       // n0, n1, n2, narr of the x grid whose line exponents
+                                      // the exact tensor-core steps share (0: none)
 };
 
 // 3D MagicFilter (sfrf_ld_narr, one grid).  order == nullptr: the reference's

@@ -350,6 +350,7 @@ int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, do
         st.src2 = k == 0 ? -1 : s;
         st.S.has_dot = ekin ? 1 : 0;   // x . (a_i D2_i x), before a_x x and the partial sum
         st.dot_slot = i;
+        if (d == 3) st.exp_axis = i;
         st.S.narr = narr;
         st.S.x_arr = st.S.y_arr = tot;
         need(P, B_X, tot * narr);
@@ -360,6 +361,9 @@ int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, do
     P.y_read = a_y != 0.0 ? tot * narr : 0;
     P.has_dot = ekin ? 1 : 0;
     P.ndot = ekin ? d : 1;
+    if (d == 3) {                  // the three sweeps read x: one exponent pass for all
+        P.exp3[0] = n[0]; P.exp3[1] = n[1]; P.exp3[2] = n[2]; P.exp3[3] = narr;
+    }
     return LIBCONV_OK;
 }
 
@@ -369,6 +373,21 @@ int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, do
 int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, DevBuf &lineexp,
              double *dot_dev, int *status, cudaStream_t st) {
     if (!valid_mode(t_mode)) return fail(LIBCONV_EMODE, "unknown mode %d", t_mode);
+    // exact tensor-core sweeps of one grid along its three axes: the line
+    // exponents of all three come from one read of x
+    int *shared_exp = nullptr;
+    long long exp_off[3] = {0, 0, 0};
+    if (t_mode == LIBCONV_MODE_TC_EXACT && P.exp3[0] > 0) {
+        const long long n0 = P.exp3[0], n1 = P.exp3[1], n2 = P.exp3[2], na = P.exp3[3];
+        exp_off[1] = n1 * n2 * na;
+        exp_off[2] = exp_off[1] + n0 * n2 * na;
+        int rc = ensure(lineexp, (size_t)(exp_off[2] + n0 * n1 * na) * sizeof(int));
+        if (rc) return rc;
+        shared_exp = (int *)lineexp.p;
+        cudaError_t e = launch_line_exp3(bufs[B_X], (int)n0, (int)n1, (int)n2, (int)na, shared_exp,
+                                         shared_exp + exp_off[1], shared_exp + exp_off[2], st);
+        if (e != cudaSuccess) return cuda_fail(e, "line exponent launch");
+    }
     for (const PlanStep &ps : P.steps) {
         Sweep S = ps.S;
         S.x = bufs[ps.src];
@@ -405,12 +424,16 @@ int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, DevBuf &line
             else tc_filter_split(h_ftab + S.ftab, flat, S.has_a ? S.a : 1.0, sch, F);
             S.has_a = 0;   // folded into the filter operands
             int *lineE = nullptr;
-            if (sch == SCH_EXACT) {
+            const bool shared = sch == SCH_EXACT && shared_exp && ps.exp_axis >= 0 && ps.src == B_X;
+            if (shared) {
+                lineE = shared_exp + exp_off[ps.exp_axis];
+            } else if (sch == SCH_EXACT) {
+                if (shared_exp) return fail(LIBCONV_EARG, "plan shares line exponents but a step does not");
                 int rc = ensure(lineexp, (size_t)sweep_tc_lines(S) * sizeof(int));
                 if (rc) return rc;
                 lineE = (int *)lineexp.p;
             }
-            e = launch_sweep_tc(S, F, sch, status, lineE, st);
+            e = launch_sweep_tc(S, F, sch, status, lineE, st, shared);
         } else {
             e = launch_sweep_fp64(S, st);
         }

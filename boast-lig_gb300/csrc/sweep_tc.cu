@@ -72,9 +72,68 @@ __global__ void line_exp_kernel(const Sweep S, int plen, int *out) {
     }
 }
 
+// Per-line exponent maxima of one n0 x n1 x n2 grid (narr of them, back to
+// back) along all three axes in one read: e0[i1 + n1 (i2 + n2 a)] over i0,
+// e1[i0 + n0 (i2 + n2 a)] over i1, e2[i0 + n0 (i1 + n1 a)] over i2 -- the
+// line orders of the three non-rotating sweeps of the grid.  Block: 32 i0 x
+// 8 i1 threads, looping over i2 in chunks of 8 (8 loads in flight); e2 is a
+// thread's own maximum, e0 a warp maximum and e1 a block maximum, the last
+// two combined across blocks with atomicMax (e0, e1 zeroed first).
+constexpr int kExpChunk = 8;
+__global__ void __launch_bounds__(256)
+line_exp3_kernel(const double *__restrict__ x, int n0, int n1, int n2, int *__restrict__ e0,
+                 int *__restrict__ e1, int *__restrict__ e2) {
+    __shared__ int ys[kExpChunk][8][32];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int i0 = blockIdx.x * 32 + tx, i1 = blockIdx.y * 8 + ty;
+    const long long a = blockIdx.z;
+    const bool valid = i0 < n0 && i1 < n1;
+    const long long plane = (long long)n0 * n1;
+    const unsigned long long *xa =
+        reinterpret_cast<const unsigned long long *>(x) + a * plane * n2 + i0 + (long long)n0 * i1;
+    int zmax = 0;
+    for (int c0 = 0; c0 < n2; c0 += kExpChunk) {
+        int e[kExpChunk];
+#pragma unroll
+        for (int c = 0; c < kExpChunk; ++c)
+            e[c] = (valid && c0 + c < n2) ? (int)((xa[plane * (c0 + c)] >> 52) & 0x7FF) : 0;
+#pragma unroll
+        for (int c = 0; c < kExpChunk; ++c) {
+            zmax = max(zmax, e[c]);
+            int w = e[c];
+            for (int o = 16; o > 0; o >>= 1) w = max(w, __shfl_xor_sync(0xffffffffu, w, o));
+            if (tx == 0 && i1 < n1 && c0 + c < n2)
+                atomicMax(e0 + i1 + (long long)n1 * (c0 + c + (long long)n2 * a), w);
+            ys[c][ty][tx] = e[c];
+        }
+        __syncthreads();
+        if (ty == 0 && i0 < n0) {
+            for (int c = 0; c < kExpChunk && c0 + c < n2; ++c) {
+                int m = ys[c][0][tx];
+#pragma unroll
+                for (int r = 1; r < 8; ++r) m = max(m, ys[c][r][tx]);
+                atomicMax(e1 + i0 + (long long)n0 * (c0 + c + (long long)n2 * a), m);
+            }
+        }
+        __syncthreads();
+    }
+    if (valid) e2[i0 + (long long)n0 * (i1 + (long long)n1 * a)] = zmax;
+}
+
 }  // namespace tck
 
 long long sweep_tc_lines(const Sweep &S) { return (long long)S.nL * S.nR * S.narr; }
+
+cudaError_t launch_line_exp3(const double *x, int n0, int n1, int n2, int narr, int *e0, int *e1,
+                             int *e2, cudaStream_t st) {
+    if (n0 < 1 || n1 < 1 || n2 < 1 || narr < 1 || narr > 65535) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(e0, 0, (size_t)n1 * n2 * narr * sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(e1, 0, (size_t)n0 * n2 * narr * sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)((n0 + 31) / 32), (unsigned)((n1 + 7) / 8), (unsigned)narr);
+    tck::line_exp3_kernel<<<grid, 256, 0, st>>>(x, n0, n1, n2, e0, e1, e2);
+    return cudaGetLastError();
+}
 
 bool sweep_tc_supported(const Sweep &S) {
     if (S.kind == KCONV) return S.ntaps == 16 || S.ntaps == 17 || S.ntaps == 29;
@@ -168,9 +227,9 @@ cudaError_t launch_sweep_tc_batch(int kind, int ntaps, const Sweep *descs, const
 }
 
 cudaError_t launch_sweep_tc(const Sweep &S, const TcFilter &F, int sch, int *status, int *lineE,
-                            cudaStream_t st) {
+                            cudaStream_t st, bool lineE_ready) {
     if (sch == SCH_EXACT) {
-        if (lineE) {
+        if (lineE && !lineE_ready) {
             // positions a line's outputs read: 0..n-1, or the whole shrink input
             const int up = S.lowfil + S.ntaps - 1;
             const int plen = S.bc == BC_SHRINK ? S.qhi + up - S.in_lo + 1 : S.n;
