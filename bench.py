@@ -116,7 +116,8 @@ class MfKin128:
         pkg.Kernel('d_kin_narr').run(3, n, [0, 0, 0], B, hx, ho1, hw, hw, a, 0.0, 0.0)
 
     e2e_note = ('d_sfrf_ld_narr (narr=B) + d_kin_narr (narr=B), host pointers (pinned), '
-                'H2D of x and D2H of psi_r and T x inside every call')
+                'H2D of x and D2H of psi_r and T x inside every call (the library pipelines '
+                'chunks of grids: copies overlap the sweeps)')
 
     def cpu_work(self, O, x, bufs):
         y, tx, w1, w2 = bufs

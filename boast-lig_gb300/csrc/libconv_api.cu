@@ -110,8 +110,18 @@ struct DevBuf {
     size_t cap = 0;
 };
 
+// One slot of the host-pointer copy/compute pipeline: its own stream and
+// buffers, so chunks in different slots run concurrently.
+struct PipeSlot {
+    cudaStream_t stream = nullptr;
+    DevBuf buf[4];                   // x, y, w1, w2 of one chunk
+    DevBuf scratch, lineexp;
+};
+constexpr int kPipeSlots = 3;
+
 struct DevState {
     bool init = false;
+    PipeSlot pipe[kPipeSlots];       // chunked host-pointer execution (exec_host)
     cudaStream_t stream = nullptr;   // stream of the host-pointer entry points
     DevBuf buf[6];                   // x, y, w1, w2, dot partials, dot scalar
     DevBuf scratch;                  // dot partials of the *_dev entry points
@@ -476,6 +486,74 @@ int read_status(DevState &s) {
     return LIBCONV_OK;
 }
 
+// narr of a plan whose steps all work on the same narr independent arrays
+// (0 otherwise).
+int plan_narr(const Plan &P) {
+    int n = 0;
+    for (const PlanStep &ps : P.steps) {
+        if (n == 0) n = ps.S.narr;
+        else if (ps.S.narr != n) return 0;
+    }
+    return n;
+}
+
+// The same plan over narr_new of the arrays (every buffer extent is per-array
+// extent times narr).
+Plan with_narr(const Plan &P, int narr_old, int narr_new) {
+    Plan Q = P;
+    for (PlanStep &ps : Q.steps) ps.S.narr = narr_new;
+    for (int b = 0; b < 4; ++b) Q.elems[b] = P.elems[b] / narr_old * narr_new;
+    Q.y_read = P.y_read / narr_old * narr_new;
+    if (Q.exp3[0]) Q.exp3[3] = narr_new;
+    return Q;
+}
+
+// Host-pointer execution of a plan over narr independent arrays, in chunks
+// of arrays on kPipeSlots streams: the copy-in of one chunk, the sweeps of
+// another and the copy-out of a third overlap (H2D and D2H copy engines and
+// the SMs).  Chunk k runs in slot k % kPipeSlots; a slot's stream orders the
+// reuse of its buffers.
+int exec_host_pipelined(const Plan &P, int narr, const double *x, double *y, DevState &s) {
+    const size_t xs = P.elems[B_X] / narr, ys = P.elems[B_Y] / narr;
+    const size_t per = (xs + ys) * sizeof(double);
+    int c = (narr + 7) / 8;
+    while ((size_t)c * per < (1u << 20) && c < narr) ++c;   // at least 1 MB per chunk
+    const int nchunk = (narr + c - 1) / c, rem = narr - (nchunk - 1) * c;
+    const Plan Qc = with_narr(P, narr, c), Qr = with_narr(P, narr, rem);
+    int rc;
+    for (int k = 0; k < kPipeSlots && k < nchunk; ++k) {
+        PipeSlot &ps = s.pipe[k];
+        if (!ps.stream) {
+            cudaError_t e = cudaStreamCreateWithFlags(&ps.stream, cudaStreamNonBlocking);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+        }
+        for (int b = 0; b < 4; ++b)
+            if (Qc.elems[b] && (rc = ensure(ps.buf[b], Qc.elems[b] * sizeof(double)))) return rc;
+    }
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < nchunk && e == cudaSuccess; ++k) {
+        PipeSlot &ps = s.pipe[k % kPipeSlots];
+        const Plan &Q = k == nchunk - 1 ? Qr : Qc;
+        const size_t a0 = (size_t)k * c, ca = k == nchunk - 1 ? rem : c;
+        double *bufs[4];
+        for (int b = 0; b < 4; ++b) bufs[b] = Q.elems[b] ? (double *)ps.buf[b].p : nullptr;
+        e = cudaMemcpyAsync(bufs[B_X], x + a0 * xs, ca * xs * sizeof(double), cudaMemcpyHostToDevice,
+                            ps.stream);
+        if (e == cudaSuccess && P.y_read)
+            e = cudaMemcpyAsync(bufs[B_Y], y + a0 * ys, ca * ys * sizeof(double),
+                                cudaMemcpyHostToDevice, ps.stream);
+        if (e != cudaSuccess) break;
+        if ((rc = run_plan(Q, bufs, ps.scratch, ps.lineexp, nullptr, (int *)s.status.p, ps.stream)))
+            return rc;
+        e = cudaMemcpyAsync(y + a0 * ys, bufs[B_Y], ca * ys * sizeof(double), cudaMemcpyDeviceToHost,
+                            ps.stream);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "pipelined copy");
+    for (int k = 0; k < kPipeSlots && k < nchunk; ++k)
+        if ((e = cudaStreamSynchronize(s.pipe[k].stream)) != cudaSuccess) return cuda_fail(e, "synchronize");
+    return read_status(s);
+}
+
 // Host-pointer execution: stage in device buffers owned by the library.
 int exec_host(const Plan &P, const double *x, double *y, double *dot_host) {
     if (!x || !y) return fail(LIBCONV_EARG, "x/y must not be null");
@@ -484,6 +562,11 @@ int exec_host(const Plan &P, const double *x, double *y, double *dot_host) {
     int rc;
     DevState *s = dev_state(rc);
     if (!s) return rc;
+    // independent arrays, no dot, at least 4 MB of input: pipelined chunks
+    const int narr = plan_narr(P);
+    if (!P.has_dot && narr >= 2 && P.elems[B_X] % narr == 0 && P.elems[B_Y] % narr == 0 &&
+        P.y_read % narr == 0 && P.elems[B_X] * sizeof(double) >= (4u << 20))
+        return exec_host_pipelined(P, narr, x, y, *s);
     for (int b = 0; b < 4; ++b)
         if (P.elems[b] && (rc = ensure(s->buf[b], P.elems[b] * sizeof(double)))) return rc;
     if (P.has_dot && (rc = ensure(s->dscalar, sizeof(double) * P.ndot))) return rc;

@@ -1,0 +1,89 @@
+"""Host-pointer calls over several arrays run as a pipeline of chunks of
+arrays (copy-in, sweeps and copy-out of different chunks overlapping on
+separate streams).  The chunks run the same kernels on the same arrays, so
+the results must equal the device-pointer call over all arrays at once bit
+for bit: checked for MagicFilter grow with ld padding, 3D kinetic with a_y,
+wavelet synthesis and a 1D sweep with a_y, including an uneven last chunk."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True, params=['fp64', 'tc_exact'])
+def compute_mode(request, pkg):
+    m = pkg.MODE_FP64 if request.param == 'fp64' else pkg.MODE_TC_EXACT
+    with pkg.mode(m):
+        yield request.param
+
+
+def rnd(seed, size):
+    return np.random.default_rng(seed).uniform(-1.0, 1.0, size)
+
+
+def dev_run(kernel, args, outs):
+    """Run the _dev form with every numpy array in args on the device; return
+    the arrays at positions `outs` back on the host."""
+    import torch
+    dargs = [torch.from_numpy(a).cuda() if isinstance(a, np.ndarray) else a for a in args]
+    kernel.run_dev(*dargs)
+    torch.cuda.synchronize()
+    return [dargs[i].cpu().numpy() for i in outs]
+
+
+def test_magicfilter_grow_ld_narr9(pkg):
+    n = [40, 36, 44]
+    nx = list(n)
+    ny = [v + 15 for v in n]
+    ny[0] += 3                                  # ld padding of the output, kept as the caller had it
+    narr = 9                                    # 9 arrays: chunks of 2 and a last chunk of 1
+    N, M = int(np.prod(nx)), int(np.prod(ny))
+    x = rnd(1, narr * N)
+    y0 = rnd(2, narr * M)
+    yh = y0.copy()
+    k = pkg.Kernel('d_sfrf_ld_narr')
+    k.run(3, n, [1, 1, 1], nx, ny, narr, x, yh, np.zeros(1), np.zeros(1))
+    w = np.zeros(narr * M * 2)
+    yd, = dev_run(k, [3, n, [1, 1, 1], nx, ny, narr, x, y0.copy(), w, w.copy()], [7])
+    assert np.array_equal(yh, yd)
+
+
+def test_kinetic_narr_with_ay(pkg):
+    n = [64, 60, 56]
+    narr = 5
+    N = int(np.prod(n))
+    x = rnd(3, narr * N)
+    y0 = rnd(4, narr * N)
+    a = [-1.3, -2.0, -0.7]
+    yh = y0.copy()
+    k = pkg.Kernel('d_kin_narr')
+    k.run(3, n, [0, 2, 0], narr, x, yh, np.zeros(1), np.zeros(1), a, 0.25, 0.5)
+    w = np.zeros(narr * N)
+    yd, = dev_run(k, [3, n, [0, 2, 0], narr, x, y0.copy(), w, w.copy(), a, 0.25, 0.5], [5])
+    assert np.array_equal(yh, yd)
+
+
+def test_wavelet_synthesis_narr(pkg):
+    n = [32, 30, 28]
+    narr = 4
+    N = 8 * int(np.prod(n))
+    x = rnd(5, narr * N)
+    yh = np.zeros(narr * N)
+    k = pkg.Kernel('d_idwt_sym8_narr')
+    k.run(3, n, [0, 0, 0], narr, x, yh, np.zeros(1), np.zeros(1))
+    w = np.zeros(narr * N)
+    yd, = dev_run(k, [3, n, [0, 0, 0], narr, x, np.zeros(narr * N), w, w.copy()], [5])
+    assert np.array_equal(yh, yd)
+
+
+def test_1d_sweep_with_ay_narr(pkg):
+    n = [96, 80, 70]
+    narr = 3
+    N = int(np.prod(n))
+    x = rnd(6, narr * N)
+    y0 = rnd(7, narr * N)
+    yh = y0.copy()
+    k = pkg.Kernel('d_s0s0_1d_sym8_md')
+    k.run(3, 1, n, 0, n, n, narr, x, yh, 1.5, 0.0, -0.25)
+    yd, = dev_run(k, [3, 1, n, 0, n, n, narr, x, y0.copy(), 1.5, 0.0, -0.25], [8])
+    assert np.array_equal(yh, yd)
