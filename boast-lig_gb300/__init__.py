@@ -284,15 +284,22 @@ def hamiltonian_sizes(n, bc, norb=1):
     return tuple(o.value for o in out)
 
 
-def hamiltonian_narr(n, bc, a_kin, norb, psig, pot, rho=None):
+def hamiltonian_narr(n, bc, a_kin, norb, psig, pot, rho=None, hpsig=None, energies=None):
     """libconv_hamiltonian_narr on host arrays: norb orbitals back to back in
     psig, one potential.  Returns (hpsig, energies[norb, 4]) with rows
-    [ekin_x, ekin_y, ekin_z, epot]; rho, when given, is updated in place."""
+    [ekin_x, ekin_y, ekin_z, epot]; rho, when given, is updated in place.
+    hpsig / energies may be given (e.g. page-locked arrays, which let the
+    library overlap the copies of chunks of orbitals with their sweeps)."""
     nsig, nreal, _ = hamiltonian_sizes(n, bc, norb)
     if psig.size != norb * nsig or pot.size != nreal or (rho is not None and rho.size != nreal):
         raise ValueError(f'psig needs {norb * nsig} and pot/rho {nreal} elements')
-    hpsig = np.zeros(norb * nsig)
-    en = np.zeros((norb, 4))
+    if hpsig is None:
+        hpsig = np.zeros(norb * nsig)
+    elif hpsig.size != norb * nsig:
+        raise ValueError(f'hpsig needs {norb * nsig} elements')
+    en = np.zeros((norb, 4)) if energies is None else energies
+    if en.size != 4 * norb:
+        raise ValueError(f'energies needs {4 * norb} elements')
     st = _ham_lib().libconv_hamiltonian_narr(
         _ints(n), _ints(bc), _dbls(a_kin), int(norb), _host_ptr(psig, False),
         _host_ptr(pot, False), _host_ptr(rho, True), _host_ptr(hpsig, True), _host_ptr(en, True))

@@ -486,6 +486,18 @@ int read_status(DevState &s) {
     return LIBCONV_OK;
 }
 
+// Page-locked host memory (cudaHostAlloc / cudaHostRegister): asynchronous
+// copies to and from it overlap kernels; pageable memory is staged by the
+// driver, so chunked copies would only add overhead.
+bool pinned(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 // narr of a plan whose steps all work on the same narr independent arrays
 // (0 otherwise).
 int plan_narr(const Plan &P) {
@@ -565,7 +577,8 @@ int exec_host(const Plan &P, const double *x, double *y, double *dot_host) {
     // independent arrays, no dot, at least 4 MB of input: pipelined chunks
     const int narr = plan_narr(P);
     if (!P.has_dot && narr >= 2 && P.elems[B_X] % narr == 0 && P.elems[B_Y] % narr == 0 &&
-        P.y_read % narr == 0 && P.elems[B_X] * sizeof(double) >= (4u << 20))
+        P.y_read % narr == 0 && P.elems[B_X] * sizeof(double) >= (4u << 20) && pinned(x) &&
+        pinned(y))
         return exec_host_pipelined(P, narr, x, y, *s);
     for (int b = 0; b < 4; ++b)
         if (P.elems[b] && (rc = ensure(s->buf[b], P.elems[b] * sizeof(double)))) return rc;
@@ -673,16 +686,96 @@ int run_ham(const Ham &H, const double *psig, const double *pot, double *rho, do
     return run_plan(H.dwt, b_dwt, s.scratch, s.lineexp, nullptr, status, st);
 }
 
+// Host-pointer form over many orbitals: chunks of orbitals pipelined on three
+// streams -- copy-in of psig (two staging buffers), the pipeline of each
+// chunk in order on one compute stream (so rho accumulates the orbitals in
+// order, as one call does), copy-out of hpsig -- chained by events.
+int ham_host_pipelined(const Ham &H, const int *n, const int *bc, const double *a_kin,
+                       const double *psig, const double *pot, double *rho, double *hpsig,
+                       double *energies, DevState &s) {
+    const int norb = H.norb;
+    const int c = (norb + 7) / 8, nchunk = (norb + c - 1) / c, rem = norb - (nchunk - 1) * c;
+    Ham Hc, Hr;
+    int rc = plan_ham(n, bc, a_kin, c, Hc);
+    if (!rc) rc = plan_ham(n, bc, a_kin, rem, Hr);
+    if (rc) return rc;
+    const size_t ns = H.nsig, nc = (size_t)c * ns;
+    const size_t nd = (rho ? 2 : 1) * H.nreal + Hc.nwork() + 4 * nc + 4 * (size_t)norb;
+    if ((rc = ensure(s.hbuf, nd * sizeof(double)))) return rc;
+    double *d_pot = (double *)s.hbuf.p, *d_rho = rho ? d_pot + H.nreal : nullptr;
+    double *d_work = d_pot + (rho ? 2 : 1) * H.nreal;
+    double *d_in[2] = {d_work + Hc.nwork(), d_work + Hc.nwork() + nc};
+    double *d_out[2] = {d_in[1] + nc, d_in[1] + 2 * nc};
+    double *d_en = d_out[1] + nc;
+    for (int k = 0; k < 3; ++k)
+        if (!s.pipe[k].stream) {
+            cudaError_t e = cudaStreamCreateWithFlags(&s.pipe[k].stream, cudaStreamNonBlocking);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+        }
+    cudaStream_t sin = s.pipe[0].stream, scomp = s.pipe[1].stream, sout = s.pipe[2].stream;
+    std::vector<cudaEvent_t> ev(3 * nchunk + 1, nullptr);   // in[k], done[k], out[k], pot
+    cudaError_t e = cudaSuccess;
+    for (size_t i = 0; i < ev.size() && e == cudaSuccess; ++i)
+        e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
+    auto cleanup = [&]() { for (cudaEvent_t x : ev) if (x) cudaEventDestroy(x); };
+    if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "cudaEventCreate"); }
+    cudaEvent_t *ev_in = ev.data(), *ev_done = ev_in + nchunk, *ev_out = ev_done + nchunk;
+    cudaEvent_t ev_pot = ev[3 * nchunk];
+    e = cudaMemcpyAsync(d_pot, pot, H.nreal * sizeof(double), cudaMemcpyHostToDevice, sin);
+    if (e == cudaSuccess && rho)
+        e = cudaMemcpyAsync(d_rho, rho, H.nreal * sizeof(double), cudaMemcpyHostToDevice, sin);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_pot, sin);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(scomp, ev_pot, 0);
+    for (int k = 0; k < nchunk && e == cudaSuccess && !rc; ++k) {
+        const Ham &Q = k == nchunk - 1 ? Hr : Hc;
+        const size_t a0 = (size_t)k * c, ca = (size_t)Q.norb;
+        const int b = k & 1;
+        // staging buffer b: its previous chunk (k - 2) must have been consumed
+        if (k >= 2) e = cudaStreamWaitEvent(sin, ev_done[k - 2], 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_in[b], psig + a0 * ns, ca * ns * sizeof(double),
+                                cudaMemcpyHostToDevice, sin);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_in[k], sin);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(scomp, ev_in[k], 0);
+        if (e == cudaSuccess && k >= 2) e = cudaStreamWaitEvent(scomp, ev_out[k - 2], 0);
+        if (e != cudaSuccess) break;
+        rc = run_ham(Q, d_in[b], d_pot, d_rho, d_out[b], d_work, d_en + 4 * a0, s, scomp);
+        if (rc) break;
+        e = cudaEventRecord(ev_done[k], scomp);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(sout, ev_done[k], 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(hpsig + a0 * ns, d_out[b], ca * ns * sizeof(double),
+                                cudaMemcpyDeviceToHost, sout);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_out[k], sout);
+    }
+    if (e == cudaSuccess && !rc) {
+        e = cudaStreamWaitEvent(sout, ev_done[nchunk - 1], 0);
+        if (e == cudaSuccess && rho)
+            e = cudaMemcpyAsync(rho, d_rho, H.nreal * sizeof(double), cudaMemcpyDeviceToHost, sout);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(energies, d_en, 4 * (size_t)norb * sizeof(double),
+                                cudaMemcpyDeviceToHost, sout);
+    }
+    for (int k = 0; k < 3; ++k) cudaStreamSynchronize(s.pipe[k].stream);
+    cleanup();
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "pipelined Hamiltonian");
+    return read_status(s);
+}
+
 // Host-pointer form: stage in the library's device buffer, run, copy back.
 // energies: 4 doubles per orbital (host).
 int ham_host(const Ham &H, const double *psig, const double *pot, double *rho, double *hpsig,
-             double *energies) {
+             double *energies, const int *n = nullptr, const int *bc = nullptr,
+             const double *a_kin = nullptr) {
     if (!psig || !pot || !hpsig || !energies)
         return fail(LIBCONV_EARG, "psig/pot/hpsig/energies must not be null");
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     int rc;
     DevState *s = dev_state(rc);
     if (!s) return rc;
+    if (n && H.norb >= 4 && pinned(psig) && pinned(hpsig))
+        return ham_host_pipelined(H, n, bc, a_kin, psig, pot, rho, hpsig, energies, *s);
     const size_t no = (size_t)H.norb, ns = no * H.nsig;
     const size_t nd = 2 * ns + (rho ? 2 : 1) * H.nreal + H.nwork() + 4 * no;
     if ((rc = ensure(s->hbuf, nd * sizeof(double)))) return rc;
@@ -1207,7 +1300,7 @@ int libconv_hamiltonian_narr(const int *n, const int *bc, const double *a_kin, i
                              double *energies) {
     Ham H;
     int rc = plan_ham(n, bc, a_kin, norb, H);
-    return rc ? rc : ham_host(H, psig, pot, rho, hpsig, energies);
+    return rc ? rc : ham_host(H, psig, pot, rho, hpsig, energies, n, bc, a_kin);
 }
 
 int libconv_hamiltonian_narr_dev(const int *n, const int *bc, const double *a_kin, int norb,

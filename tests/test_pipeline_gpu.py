@@ -1,13 +1,27 @@
-"""Host-pointer calls over several arrays run as a pipeline of chunks of
-arrays (copy-in, sweeps and copy-out of different chunks overlapping on
-separate streams).  The chunks run the same kernels on the same arrays, so
-the results must equal the device-pointer call over all arrays at once bit
-for bit: checked for MagicFilter grow with ld padding, 3D kinetic with a_y,
-wavelet synthesis and a 1D sweep with a_y, including an uneven last chunk."""
+"""Host-pointer calls over several arrays in page-locked memory run as a
+pipeline of chunks of arrays (copy-in, sweeps and copy-out of different
+chunks overlapping on separate streams).  The chunks run the same kernels on
+the same arrays, so the results must equal the device-pointer call over all
+arrays at once bit for bit: checked for MagicFilter grow with ld padding, 3D
+kinetic with a_y, wavelet synthesis and a 1D sweep with a_y, including an
+uneven last chunk; and the local Hamiltonian over orbitals against
+single-orbital calls."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+_KEEP = []
+
+
+def pinned(a):
+    """Page-locked copy of a float64 array (the tensor is kept alive)."""
+    import torch
+    t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+    _KEEP.append(t)
+    v = t.numpy()
+    v[:] = a.ravel()
+    return v
 
 
 @pytest.fixture(autouse=True, params=['fp64', 'tc_exact'])
@@ -40,9 +54,9 @@ def test_magicfilter_grow_ld_narr9(pkg):
     N, M = int(np.prod(nx)), int(np.prod(ny))
     x = rnd(1, narr * N)
     y0 = rnd(2, narr * M)
-    yh = y0.copy()
+    yh = pinned(y0)
     k = pkg.Kernel('d_sfrf_ld_narr')
-    k.run(3, n, [1, 1, 1], nx, ny, narr, x, yh, np.zeros(1), np.zeros(1))
+    k.run(3, n, [1, 1, 1], nx, ny, narr, pinned(x), yh, np.zeros(1), np.zeros(1))
     w = np.zeros(narr * M * 2)
     yd, = dev_run(k, [3, n, [1, 1, 1], nx, ny, narr, x, y0.copy(), w, w.copy()], [7])
     assert np.array_equal(yh, yd)
@@ -55,9 +69,9 @@ def test_kinetic_narr_with_ay(pkg):
     x = rnd(3, narr * N)
     y0 = rnd(4, narr * N)
     a = [-1.3, -2.0, -0.7]
-    yh = y0.copy()
+    yh = pinned(y0)
     k = pkg.Kernel('d_kin_narr')
-    k.run(3, n, [0, 2, 0], narr, x, yh, np.zeros(1), np.zeros(1), a, 0.25, 0.5)
+    k.run(3, n, [0, 2, 0], narr, pinned(x), yh, np.zeros(1), np.zeros(1), a, 0.25, 0.5)
     w = np.zeros(narr * N)
     yd, = dev_run(k, [3, n, [0, 2, 0], narr, x, y0.copy(), w, w.copy(), a, 0.25, 0.5], [5])
     assert np.array_equal(yh, yd)
@@ -68,9 +82,9 @@ def test_wavelet_synthesis_narr(pkg):
     narr = 4
     N = 8 * int(np.prod(n))
     x = rnd(5, narr * N)
-    yh = np.zeros(narr * N)
+    yh = pinned(np.zeros(narr * N))
     k = pkg.Kernel('d_idwt_sym8_narr')
-    k.run(3, n, [0, 0, 0], narr, x, yh, np.zeros(1), np.zeros(1))
+    k.run(3, n, [0, 0, 0], narr, pinned(x), yh, np.zeros(1), np.zeros(1))
     w = np.zeros(narr * N)
     yd, = dev_run(k, [3, n, [0, 0, 0], narr, x, np.zeros(narr * N), w, w.copy()], [5])
     assert np.array_equal(yh, yd)
@@ -82,8 +96,32 @@ def test_1d_sweep_with_ay_narr(pkg):
     N = int(np.prod(n))
     x = rnd(6, narr * N)
     y0 = rnd(7, narr * N)
-    yh = y0.copy()
+    yh = pinned(y0)
     k = pkg.Kernel('d_s0s0_1d_sym8_md')
-    k.run(3, 1, n, 0, n, n, narr, x, yh, 1.5, 0.0, -0.25)
+    k.run(3, 1, n, 0, n, n, narr, pinned(x), yh, 1.5, 0.0, -0.25)
     yd, = dev_run(k, [3, 1, n, 0, n, n, narr, x, y0.copy(), 1.5, 0.0, -0.25], [8])
     assert np.array_equal(yh, yd)
+
+
+def test_hamiltonian_orbitals_pipelined(pkg):
+    """9 orbitals in page-locked memory (chunks of 2 and a last one of 1):
+    every orbital's hpsig and the accumulated rho equal single-orbital calls
+    made in order, bit for bit; the energies agree to 1e-12."""
+    n, bc, norb = [10, 9, 11], [2, 2, 2], 9
+    a = [-1.2, -0.8, -1.6]
+    nsig, nreal, _ = pkg.hamiltonian_sizes(n, bc)
+    rng = np.random.default_rng(40)
+    psig = pinned(rng.standard_normal(norb * nsig))
+    pot = rng.uniform(-1.0, 2.0, nreal)
+    rho0 = rng.uniform(0.0, 1.0, nreal)
+    rb = pinned(rho0)
+    hb, eb = pkg.hamiltonian_narr(n, bc, a, norb, psig, pot, rb, hpsig=pinned(np.zeros(norb * nsig)),
+                                  energies=pinned(np.zeros(4 * norb)).reshape(norb, 4))
+    rs = rho0.copy()
+    for j in range(norb):
+        sl = slice(j * nsig, (j + 1) * nsig)
+        hs, es, ps = pkg.hamiltonian(n, bc, a, np.array(psig[sl]), pot, rs)
+        assert np.array_equal(hb[sl], hs), j
+        assert np.abs(eb[j, :3] - es).max() <= 1e-12 * np.abs(es).max()
+        assert abs(eb[j, 3] - ps) <= 1e-12 * np.abs(pot).max() * float(np.abs(psig[sl]) @ np.abs(psig[sl])) * 2
+    assert np.array_equal(rb, rs)
