@@ -70,6 +70,67 @@ def peaks():
             'source': 'measured' if d else 'fallback'}
 
 
+class Ranks:
+    """One process per GPU (torchrun): rank, world size and local GPU from the
+    environment, a process group when world > 1 (NCCL on GPUs, gloo for the
+    CPU tests), and the barrier / max / sum the runs need.  Nothing on the
+    data path is collective: the ranks only agree on times and totals."""
+
+    def __init__(self, backend='nccl'):
+        import torch
+        self.world = int(os.environ.get('WORLD_SIZE', '1'))
+        self.rank = int(os.environ.get('RANK', '0'))
+        self.local = int(os.environ.get('LOCAL_RANK', '0'))
+        if backend == 'nccl':
+            torch.cuda.set_device(self.local)
+            self.device = torch.device('cuda', self.local)
+        else:
+            self.device = torch.device('cpu')
+        if self.world > 1:
+            import torch.distributed as dist
+            if backend == 'nccl':
+                dist.init_process_group('nccl', device_id=self.device)
+            else:
+                dist.init_process_group(backend)
+
+    def barrier(self):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def _reduce(self, v, op):
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(v)], dtype=torch.float64, device=self.device)
+        dist.all_reduce(t, op=op)
+        return t.item()
+
+    def max(self, v):
+        if self.world == 1:
+            return float(v)
+        import torch.distributed as dist
+        return self._reduce(v, dist.ReduceOp.MAX)
+
+    def sum(self, v):
+        if self.world == 1:
+            return float(v)
+        import torch.distributed as dist
+        return self._reduce(v, dist.ReduceOp.SUM)
+
+    def close(self):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+def shard_balanced(sizes, rank, world):
+    """Indices of the items rank takes: items in decreasing size dealt round
+    robin (ties by index), so each rank's total is within one item of the
+    others'."""
+    order = sorted(range(len(sizes)), key=lambda g: (-sizes[g], g))
+    return [g for i, g in enumerate(order) if i % world == rank]
+
+
 def package():
     import __graft_entry__ as ge
     return ge.package()
@@ -647,19 +708,12 @@ def run_orbitals(args, W):
     same operators called grid by grid through the single-grid entry points."""
     import torch
     pkg = package()
-    world = int(os.environ.get('WORLD_SIZE', '1'))
-    rank = int(os.environ.get('RANK', '0'))
-    local = int(os.environ.get('LOCAL_RANK', '0'))
-    torch.cuda.set_device(local)
-    dev = torch.device('cuda', local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group('nccl', device_id=dev)
+    R = Ranks()
+    world, rank, local, dev = R.world, R.rank, R.local, R.device
     dims_all = W.dims()
     xs_all = W.base()
     # orbitals are partitioned across ranks, balanced by size (largest first)
-    order = sorted(range(len(dims_all)), key=lambda g: -int(np.prod(dims_all[g])))
-    mine = [g for i, g in enumerate(order) if i % world == rank]
+    mine = shard_balanced([int(np.prod(d)) for d in dims_all], rank, world)
     dims = [dims_all[g] for g in mine]
     xs = [xs_all[g] for g in mine]
     pkg.set_mode(getattr(pkg, MODES[args.mode]))
@@ -678,10 +732,7 @@ def run_orbitals(args, W):
         B.run(x, y_mf, y_kin, stream=stream)
     pkg.check(stream)
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+    barrier = R.barrier
 
     clocks = Clocks(local)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -697,16 +748,8 @@ def run_orbitals(args, W):
     ck = clocks.stop()
     pkg.check(stream)
     ms = start.elapsed_time(stop)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = t.item()
-        tot = torch.tensor([float(n_in)], device=dev)
-        dist.all_reduce(tot)
-        pts_step = tot.item()
-    else:
-        pts_step = n_in
+    ms = R.max(ms)
+    pts_step = R.sum(n_in)               # input points of all ranks' orbitals
     value = pts_step * args.steps / (ms / 1e3)
 
     # the same work grid by grid through the single-grid device entry points
@@ -801,9 +844,7 @@ def run_orbitals(args, W):
     if rank == 0:
         print(json.dumps(line), flush=True)
     B.close()
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    R.close()
 
 
 def run_precond(args, W):
@@ -813,14 +854,8 @@ def run_precond(args, W):
     import torch
     pkg = package()
     from boast_lig_gb300 import precond as P
-    world = int(os.environ.get('WORLD_SIZE', '1'))
-    rank = int(os.environ.get('RANK', '0'))
-    local = int(os.environ.get('LOCAL_RANK', '0'))
-    torch.cuda.set_device(local)
-    dev = torch.device('cuda', local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group('nccl', device_id=dev)
+    R = Ranks()
+    world, rank, local, dev = R.world, R.rank, R.local, R.device
     pkg.set_mode(getattr(pkg, MODES[args.mode if args.mode in ('fp64', 'tc_exact') else 'tc_exact']))
     net = P.Net.load(os.path.join(P.WEIGHTS_DIR, W.weights), device=dev)
     b_np, eps_np = W.systems()
@@ -831,10 +866,7 @@ def run_precond(args, W):
     x = torch.empty_like(b)
     stream = torch.cuda.Stream(device=dev)
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+    barrier = R.barrier
 
     def timed(m, steps):
         for _ in range(max(args.warmup, 3) if m is net else 1):
@@ -858,11 +890,7 @@ def run_precond(args, W):
     ck = clocks.stop()
     ms_plain, it_p, res_p, _ = timed(None, max(1, min(args.steps, 3)))
     steps_plain = max(1, min(args.steps, 3))
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = t.item()
+    ms = R.max(ms)
     value = nsys * world * args.steps / (ms / 1e3)
     plain = nsys * steps_plain / (ms_plain / 1e3)
 
@@ -934,9 +962,7 @@ def run_precond(args, W):
                                           'one system per host thread at a time'}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    R.close()
 
 
 def run_hamiltonian(args, W):
@@ -945,14 +971,8 @@ def run_hamiltonian(args, W):
     over the orbitals, per-orbital energies kept on the device)."""
     import torch
     pkg = package()
-    world = int(os.environ.get('WORLD_SIZE', '1'))
-    rank = int(os.environ.get('RANK', '0'))
-    local = int(os.environ.get('LOCAL_RANK', '0'))
-    torch.cuda.set_device(local)
-    dev = torch.device('cuda', local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group('nccl', device_id=dev)
+    R = Ranks()
+    world, rank, local, dev = R.world, R.rank, R.local, R.device
     pkg.set_mode(getattr(pkg, MODES[args.mode]))
     nsig, nreal, nwork = pkg.hamiltonian_sizes(W.n, W.bc)
     B = args.grids
@@ -1001,10 +1021,7 @@ def run_hamiltonian(args, W):
     del H1
     step()
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+    barrier = R.barrier
 
     clocks = Clocks(local)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -1021,11 +1038,7 @@ def run_hamiltonian(args, W):
     ck = clocks.stop()
     pkg.check(sp)
     ms = start.elapsed_time(stop)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = t.item()
+    ms = R.max(ms)
     value = B * world * args.steps / (ms / 1e3)
     en = H.energies.cpu().numpy()
 
@@ -1100,9 +1113,7 @@ def run_hamiltonian(args, W):
                                           'orbital per host thread'}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    R.close()
 
 
 def run_poisson(args, W):
@@ -1111,14 +1122,8 @@ def run_poisson(args, W):
     import ctypes
     import torch
     pkg = package()
-    world = int(os.environ.get('WORLD_SIZE', '1'))
-    rank = int(os.environ.get('RANK', '0'))
-    local = int(os.environ.get('LOCAL_RANK', '0'))
-    torch.cuda.set_device(local)
-    dev = torch.device('cuda', local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group('nccl', device_id=dev)
+    R = Ranks()
+    world, rank, local, dev = R.world, R.rank, R.local, R.device
     pkg.set_mode(getattr(pkg, MODES[args.mode]))
     n = W.n
     N = int(np.prod(n))
@@ -1148,10 +1153,7 @@ def run_poisson(args, W):
     stream.synchronize()
     pkg.check(stream)
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+    barrier = R.barrier
 
     clocks = Clocks(local)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -1168,11 +1170,7 @@ def run_poisson(args, W):
     ck = clocks.stop()
     pkg.check(stream)
     ms = start.elapsed_time(stop)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = t.item()
+    ms = R.max(ms)
     value = N * world * args.steps / (ms / 1e3)
 
     # one derivative sweep timed alone (the dominant kernel): d/dz of u0
@@ -1246,9 +1244,7 @@ def run_poisson(args, W):
                                           'oracle_div_u_i with cc, one grid per host thread'}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    R.close()
 
 
 def run_gpu(args):
@@ -1263,14 +1259,8 @@ def run_gpu(args):
         return run_orbitals(args, W)
     if W.name == 'precond256':
         return run_precond(args, W)
-    world = int(os.environ.get('WORLD_SIZE', '1'))
-    rank = int(os.environ.get('RANK', '0'))
-    local = int(os.environ.get('LOCAL_RANK', '0'))
-    torch.cuda.set_device(local)
-    dev = torch.device('cuda', local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group('nccl', device_id=dev)
+    R = Ranks()
+    world, rank, local, dev = R.world, R.rank, R.local, R.device
     B = args.grids
     Ni, No = W.n_in, W.n_out
     base = W.base(4)
@@ -1298,10 +1288,7 @@ def run_gpu(args):
     stream.synchronize()
     pkg.check(sp)
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+    barrier = R.barrier
 
     clocks = Clocks(local)
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(len(ops) + 1)]
@@ -1321,11 +1308,7 @@ def run_gpu(args):
     pkg.check(sp)
     ms = start.elapsed_time(stop)
     op_ms = [sum(e[i].elapsed_time(e[i + 1]) for e in evs) for i in range(len(ops))]
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = t.item()
+    ms = R.max(ms)
     pts_step = B * Ni * world
     value = pts_step * args.steps / (ms / 1e3)
 
@@ -1412,9 +1395,7 @@ def run_gpu(args):
         line['cpu_baseline'] = cpu_baseline_sample(W, base)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    R.close()
 
 
 def main():
