@@ -292,13 +292,16 @@ class Orbitals512:
 class Precond256:
     """256 shifted kinetic solves (T - eps) x = b on 48^3 periodic grids."""
     name = 'precond256'
-    metric = ('solves/s to ||r|| <= 1e-8, 256 x 48^3 periodic (T - eps) x = b, flexible CG with '
-              'the learned preconditioner')
     n = 48
     h = 0.4
     nsys = 256
     tol = 1e-8
     weights = 'precond_n48_h0.40.npz'
+
+    @property
+    def metric(self):
+        return (f'solves/s to ||r|| <= 1e-8, {self.nsys} x 48^3 periodic (T - eps) x = b, flexible '
+                'CG with the learned preconditioner')
 
     def systems(self):
         package()
@@ -930,7 +933,15 @@ def run_precond(args, W):
     t_conv = c0.elapsed_time(c1) / 10 / 1e3
     flops = nsys * n ** 3 * 16 * 16 * 27 * 2
     pk = peaks()
-    achieved = flops / t_conv / 1e12
+    tflops = flops / t_conv / 1e12
+    # algorithmic bytes: 16 BF16 channels read and written per point
+    alg_bytes = nsys * n ** 3 * 64
+    achieved = alg_bytes / t_conv / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, 'profiles', 'precond_conv_tc_traffic.json')
+    if os.path.exists(tf):
+        with open(tf) as f:
+            traffic = json.load(f)['dram_bytes_per_point'] * nsys * n ** 3
     line = {'metric': W.metric, 'value': value, 'unit': 'solves/s', 'n_gpus': world,
             'steps': args.steps, 'warmup': max(args.warmup, 3), 'ms_per_step': ms / args.steps,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
@@ -950,10 +961,11 @@ def run_precond(args, W):
                        'learned_over_plain': value / world / plain,
                        'l2': 'working set (7 vectors x 226 MB + activations) far above L2'},
             'clocks': ck, 'e2e': e2e, 'gpu_launches': args.steps * (15 * int(it.max()) + 12),
-            'roofline': {'bound': 'tensor', 'achieved': achieved, 'peak': pk['bf16'],
-                         'unit': 'TFLOP/s', 'frac': achieved / pk['bf16'], 'traffic': None,
-                         'kernel': 'conv_kernel<ACT,ACT_RELU> (16 -> 16 channels, 3^3, '
-                                   'mma.sync bf16, 256 x 48^3 points per launch)',
+            'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': pk['hbm'],
+                         'unit': 'GB/s', 'frac': achieved / pk['hbm'], 'traffic': traffic,
+                         'tensor_tflops': tflops, 'tensor_frac': tflops / pk['bf16'],
+                         'kernel': 'conv_tc_kernel<ACT,ACT_RELU,8> (16 -> 16 channels, 3^3, '
+                                   'tcgen05 kind::f16 BF16, 256 x 48^3 points per launch)',
                          'peak_source': pk['source'], 'launch_ms': t_conv * 1e3}}
     if rank == 0 and world == 1 and not args.no_cpu:
         k, t, th = cpu_solves(W, 10.0)
@@ -1406,6 +1418,8 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--workload', default='mfkin128', choices=list(WORKLOADS))
     ap.add_argument('--grids', type=int, default=32)
+    ap.add_argument('--systems', type=int, default=None,
+                    help='precond256: number of systems (default 256; smaller for profiling)')
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline sample')
     ap.add_argument('--no-tune', action='store_true',
                     help='orbitals512: use the cached or default batch configuration')
@@ -1413,6 +1427,8 @@ def main():
                     help='tc_exact: tensor-core exact-digit sweeps (FP64-accurate); fp64: FP64 '
                          'FMA; tc_bf16x3 / tc_tf32x3: split precision (error reported)')
     args = ap.parse_args()
+    if args.systems:
+        WORKLOADS['precond256'].nsys = args.systems
     if args.impl == 'reference':
         run_reference(args)
     else:

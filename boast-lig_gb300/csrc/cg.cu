@@ -462,7 +462,8 @@ int libconv_cg_solve(int n, int nsys, const double *h, const double *eps, const 
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return lcg::report_cuda(e, "CG residual");
     }
-    return LIBCONV_OK;
+    auto lib = lcg::library_lock();
+    return lcg::host_finish(st);   // device status word of the bounded tensor-core waits
 }
 
 }  // extern "C"

@@ -21,10 +21,17 @@
 //
 // forward / input-gradient: D[point][cout] = sum_t A_t[point][cin] W_t[cout][cin]
 // weight-gradient:          dW_t[cout][cin] = sum_point G[point][cout] X[point + d_t][cin]
+//
+// For n >= 16 the forward / input-gradient convolution runs on the 5th-
+// generation tensor cores instead (conv_tc_kernel below): the halo is laid
+// out so that every tap's A operand is one shared-memory descriptor, the
+// accumulators live in TMEM.  The mma.sync kernel remains for n = 8 and for
+// the weight gradient (a reduction over points, training only).
 #include <cuda_bf16.h>
 #include <stdint.h>
 
 #include "../../include/libconv_gb300.h"
+#include "lcg_plan.cuh"
 
 namespace {
 
@@ -292,6 +299,318 @@ __global__ void reduce_parts(const float *part, int nparts, int len, float *out)
     out[i] = (float)s;
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-core (tcgen05) forward / input-gradient convolution, n >= 16.
+//
+// Output tile: 8 (x) x 16 (y) x TZ (z) points.  Its 10 x 18 x (TZ + 2) halo
+// sits in shared memory as two planes of 8-channel chunks,
+// [chunk][z][y][x] x 16 B.  For halo z-plane h and in-plane tap (dx, dy) the
+// A operand (M = 128 rows = 16 y-rows of 8 x-points, K = 16 input channels)
+// is one K-major, unswizzled descriptor into that buffer: a core matrix is 8
+// consecutive x-points x 16 B starting at halo point (dx, dy, h), the 8-row
+// groups (successive y) one halo row (160 B) apart, the two channel chunks
+// one plane apart.  The three z-taps of (dx, dy) read that same A: their
+// weights are stacked along N (rows 16 (2 - dz) + cout, dz = 0..2 the tap's
+// z offset + 1), and the contribution of halo plane h through tap dz belongs
+// to output plane h - dz, whose FP32 accumulators sit at TMEM columns
+// 16 (h - dz) + cout.  Stacked in that order, one MMA at column 16 (h - dz_max)
+// with N = 16 x (number of valid dz) adds every z-tap of (dx, dy) for plane
+// h to its own output plane; the first MMA of a plane that opens output
+// plane h is split so that block starts from zero (accumulate off) while the
+// older planes' blocks accumulate.  Per tile: 9 (TZ + 2) + TZ - 1 MMAs of
+// kind::f16 (BF16 operands, M = 128, N = 16 / 32 / 48, K = 16); each A tile
+// read from shared memory serves up to 48 output columns instead of 16.
+// Weights: per (dx, dy) a 48 x 16 K-major tile, 8-row groups 128 B apart,
+// the two K chunks 768 B apart.
+//
+// One CTA of 8 warps per tile at a time: all threads stage the halo
+// (cp.async for activations), thread 0 issues the MMAs and commits them to
+// an mbarrier, then warp w drains TMEM lanes 32 (w % 4) .. + 31 of half of
+// the output planes (bias + ReLU / mask / field scale, 32 B stored per
+// point).  Several CTAs reside per SM, so one CTA's staging overlaps
+// another's MMAs and epilogue.  Every wait is bounded; a wait that gives up
+// sets the device status word.
+namespace tcc {
+constexpr int kTX = 8, kTY = 16;
+constexpr int kHX = kTX + 2, kHY = kTY + 2;
+constexpr uint32_t kRowB = kHX * 16;              // one halo row (8-row group stride, SBO)
+constexpr uint32_t kJB = 48 * 32;                 // one (dx, dy) stack of 3 taps x 16 x 16 BF16
+constexpr uint32_t kWB = 9 * kJB;
+constexpr int kThreads = 256;
+constexpr long long kWaitCycles = 4000000000LL;   // ~2 s of SM clock
+
+template <int TZ>
+struct Geo {
+    static constexpr int HZ = TZ + 2;
+    static constexpr int HPTS = kHX * kHY * HZ;                  // halo points
+    static constexpr uint32_t PLANE = HPTS * 16;                 // one 8-channel chunk plane
+    static constexpr uint32_t HALO = 2 * PLANE;
+    static constexpr uint32_t SMEM = HALO + kWB + 16 * 4 + 16;   // + bias, mbarrier, TMEM slot
+    static constexpr uint32_t TMEM_COLS = TZ * 16 <= 32 ? 32 : TZ * 16 <= 64 ? 64 : 128;
+    static constexpr int CTAS = SMEM <= 50 * 1024 ? 4 : 3;       // resident CTAs per SM
+    static_assert(TZ % 2 == 0 && TZ * 16 <= 128, "tile depth");
+    static_assert(CTAS * TMEM_COLS <= 512, "TMEM columns");
+    static_assert(CTAS * (SMEM + 1024) <= 228 * 1024, "shared memory");
+    static_assert(2 * PLANE <= (0x3FFFu << 4), "descriptor offsets");
+};
+
+// kind::f16 instruction descriptor: D F32 (bits 4-5 = 1), A and B BF16 (bits
+// 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+__host__ __device__ constexpr uint32_t idesc(int nn) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nn >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+// Shared-memory matrix descriptor, K-major without swizzle: start address,
+// leading (K-direction) and stride (8-row group) byte offsets in 16-byte
+// units, descriptor version 1 at bits 46-47.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t accum) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(id), "r"(accum)
+        : "memory");
+}
+
+__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase of the given parity; false after ~2 s.
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
+    if (bar_try(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!bar_try(bar, parity)) {
+        __nanosleep(64);
+        if (clock64() - t0 > kWaitCycles) return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+        "%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
+}
+
+// Stage the halo of the tile whose first halo point is (x0, y0, z0) of
+// system s (periodic wrap; n >= 16 so one wrap suffices on every axis).
+template <int SRC, int TZ>
+__device__ __forceinline__ void stage(const ConvArgs &A, uint8_t *halo, int s, int x0, int y0,
+                                      int z0) {
+    using G = Geo<TZ>;
+    const int n = A.n;
+    const long long base = (long long)s * n * n * n;
+    if (SRC == SRC_ACT) {
+        const uint32_t hb = saddr(halo);
+        for (int idx = threadIdx.x; idx < 2 * G::HPTS; idx += kThreads) {
+            const int i = idx >> 1, c = idx & 1;
+            const int hx = i % kHX, hy = (i / kHX) % kHY, hz = i / (kHX * kHY);
+            const int gx = wrap(x0 + hx, n), gy = wrap(y0 + hy, n), gz = wrap(z0 + hz, n);
+            const long long p = base + gx + (long long)n * (gy + (long long)n * gz);
+            cp_async16(hb + c * G::PLANE + i * 16, A.src_act + p * 16 + c * 8);
+        }
+        asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;\n" ::: "memory");
+    } else {
+        // channels 0 (field x factor) and 1 (eps or 0) in chunk 0; chunk 1
+        // stays zero from the kernel's start
+        const double fac = A.src_fac[s];
+        const float e = SRC == SRC_FIELD_EPS ? (float)A.eps[s] : 0.f;
+        for (int i = threadIdx.x; i < G::HPTS; i += kThreads) {
+            const int hx = i % kHX, hy = (i / kHX) % kHY, hz = i / (kHX * kHY);
+            const int gx = wrap(x0 + hx, n), gy = wrap(y0 + hy, n), gz = wrap(z0 + hz, n);
+            const long long p = base + gx + (long long)n * (gy + (long long)n * gz);
+            __nv_bfloat162 h01 = __floats2bfloat162_rn((float)(A.src_field[p] * fac), e);
+            *reinterpret_cast<uint4 *>(halo + i * 16) =
+                make_uint4(*reinterpret_cast<uint32_t *>(&h01), 0u, 0u, 0u);
+        }
+    }
+}
+
+// The MMAs of one tile (thread 0).
+template <int TZ>
+__device__ __forceinline__ void issue_tile(uint32_t tmem, uint32_t hb, uint32_t wb) {
+    using G = Geo<TZ>;
+#pragma unroll 1
+    for (int h = 0; h < TZ + 2; ++h) {
+        const int dmax = h < 2 ? h : 2, dmin = h > TZ - 1 ? h - (TZ - 1) : 0;
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+            const int dx = j % 3, dy = j / 3;
+            const uint64_t a = sdesc(hb + (h * kHY + dy) * kRowB + dx * 16, G::PLANE, kRowB);
+            const uint32_t bj = wb + j * kJB;
+            if (j == 0 && h < TZ) {
+                // output plane h opens here (tap dz = 0, stack rows 32..47)
+                mma(tmem + 16 * h, a, sdesc(bj + 32 * 16, 768, 128), idesc(16), 0u);
+                if (dmax > 0)
+                    mma(tmem + 16 * (h - dmax), a, sdesc(bj + 16 * (2 - dmax) * 16, 768, 128),
+                        idesc(16 * dmax), 1u);
+            } else {
+                mma(tmem + 16 * (h - dmax), a, sdesc(bj + 16 * (2 - dmax) * 16, 768, 128),
+                    idesc(16 * (dmax - dmin + 1)), 1u);
+            }
+        }
+    }
+}
+
+}  // namespace tcc
+
+template <int SRC, int DST, int TZ>
+__global__ void __launch_bounds__(tcc::kThreads, tcc::Geo<TZ>::CTAS)
+    conv_tc_kernel(const ConvArgs A, int *status) {
+    using namespace tcc;
+    using G = Geo<TZ>;
+    extern __shared__ __align__(128) uint8_t sm[];
+    uint8_t *halo = sm;
+    uint8_t *wsm = sm + G::HALO;
+    float *bsm = reinterpret_cast<float *>(wsm + kWB);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(bsm + 16);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int n = A.n;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         saddr(tslot)),
+                     "r"(G::TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    // weights: 16-byte piece (tap t, cout co, cin chunk kc) to stack j = t % 9,
+    // row 16 (2 - dz) + co with dz = t / 9
+    for (int i = tid; i < 27 * 16 * 2; i += tcc::kThreads) {
+        const int t = i >> 5, co = (i >> 1) & 15, kc = i & 1;
+        const int row = 16 * (2 - t / 9) + co;
+        *reinterpret_cast<uint4 *>(wsm + (t % 9) * kJB + kc * 768 + row * 16) =
+            *reinterpret_cast<const uint4 *>(A.wt + (t * 16 + co) * 16 + kc * 8);
+    }
+    if (tid < 16) bsm[tid] = DST == DST_ACT_MASK ? 0.f : A.bias[tid];
+    if (SRC != SRC_ACT)
+        for (int i = tid; i < G::HPTS; i += tcc::kThreads)
+            *reinterpret_cast<uint4 *>(halo + G::PLANE + i * 16) = make_uint4(0u, 0u, 0u, 0u);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+    const uint32_t hb = saddr(halo), wb = saddr(wsm), barA = saddr(bar);
+
+    const int tpx = n / kTX, tpy = (n + kTY - 1) / kTY, tpz = n / TZ;
+    const long long per = (long long)tpx * tpy * tpz;
+    const long long ntiles = per * A.nsys;
+    const int q = warp & 3, mh = warp >> 2;
+    const int ox = lane & 7, oy = 4 * q + (lane >> 3);   // this thread's tile row 32 q + lane
+    uint32_t phase = 0;
+    bool alive = true;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int s = (int)(tile / per);
+        if (A.active && !A.active[s]) continue;   // uniform over the CTA
+        int r = (int)(tile % per);
+        const int xt = r % tpx;
+        r /= tpx;
+        const int yt = r % tpy, zt = r / tpy;
+        const int tx = xt * kTX, tz = zt * TZ;
+        // the last y tile of a grid with n % 16 == 8 overlaps the one before
+        // it; rows below ybeg were written by that tile
+        const int ty = min(yt * kTY, n - kTY), ybeg = yt * kTY - ty;
+        tcc::stage<SRC, TZ>(A, halo, s, tx - 1, ty - 1, tz - 1);
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            issue_tile<TZ>(tmem, hb, wb);
+            asm volatile(
+                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                    barA)
+                : "memory");
+        }
+        __syncwarp();
+        const bool ok = bar_wait(barA, phase);
+        phase ^= 1;
+        if (!__syncthreads_and(ok)) {
+            alive = false;
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const long long pbase = (long long)s * n * n * n + (tx + ox) + (long long)n * (ty + oy);
+        const bool store = oy >= ybeg;
+#pragma unroll 1
+        for (int mm = 0; mm < TZ / 2; ++mm) {
+            const int m = (TZ / 2) * mh + mm;
+            uint32_t v[16];
+            __syncwarp();
+            tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + m * 16, v);
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (!store) continue;   // uniform per warp (ybeg is 0 or 8, a warp holds 4 rows)
+            const long long p = pbase + (long long)n * n * (tz + m);
+            float f[16];
+#pragma unroll
+            for (int c = 0; c < 16; ++c)
+                f[c] = (A.nout_tiles == 1 && c >= 8) ? 0.f : __uint_as_float(v[c]);
+            if (DST == DST_FIELD) {
+                A.dst_field[p] = A.dst_fac[s] * (double)(f[0] + bsm[0]);
+            } else {
+                if (DST == DST_ACT_RELU) {
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) f[c] = fmaxf(f[c] + bsm[c], 0.f);
+                } else {
+                    const uint4 *mk4 = reinterpret_cast<const uint4 *>(A.mask + p * 16);
+                    const uint4 mk[2] = {mk4[0], mk4[1]};
+                    const __nv_bfloat162 *mk2 = reinterpret_cast<const __nv_bfloat162 *>(mk);
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) {
+                        if (!(__low2float(mk2[c]) > 0.f)) f[2 * c] = 0.f;
+                        if (!(__high2float(mk2[c]) > 0.f)) f[2 * c + 1] = 0.f;
+                    }
+                }
+                uint32_t o[8];
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    __nv_bfloat162 hv = __floats2bfloat162_rn(f[2 * c], f[2 * c + 1]);
+                    o[c] = *reinterpret_cast<uint32_t *>(&hv);
+                }
+                uint4 *dst = reinterpret_cast<uint4 *>(A.dst_act + p * 16);
+                dst[0] = make_uint4(o[0], o[1], o[2], o[3]);
+                dst[1] = make_uint4(o[4], o[5], o[6], o[7]);
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    }
+    if (!alive && tid == 0) atomicExch(status, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                     "r"(G::TMEM_COLS)
+                     : "memory");
+}
+
+// Tile depth of the tensor-core kernel (z-planes per tile).
+constexpr int kConvTZ = 8;
+
 int g_sms = 0;
 int sm_count() {
     if (!g_sms) {
@@ -304,7 +623,24 @@ int sm_count() {
 }
 
 template <int SRC, int DST>
-cudaError_t launch_conv(const ConvArgs &A, cudaStream_t st) {
+cudaError_t launch_conv(const ConvArgs &A, int *status, cudaStream_t st) {
+    if (A.n >= tcc::kTY) {
+        using G = tcc::Geo<kConvTZ>;
+        static bool attr = false;   // the dynamic shared memory opt-in, once per instantiation
+        if (!attr) {
+            cudaError_t e = cudaFuncSetAttribute(conv_tc_kernel<SRC, DST, kConvTZ>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)G::SMEM);
+            if (e != cudaSuccess) return e;
+            attr = true;
+        }
+        const long long tiles = (long long)A.nsys * (A.n / tcc::kTX) *
+                                ((A.n + tcc::kTY - 1) / tcc::kTY) * (A.n / kConvTZ);
+        const long long cap = (long long)G::CTAS * sm_count();
+        conv_tc_kernel<SRC, DST, kConvTZ>
+            <<<(unsigned)(tiles < cap ? tiles : cap), tcc::kThreads, G::SMEM, st>>>(A, status);
+        return cudaGetLastError();
+    }
     const int tpa = A.n / kT;
     const long long tiles = (long long)A.nsys * tpa * tpa * tpa;
     const long long grid = tiles < 4LL * sm_count() ? tiles : 4LL * sm_count();
@@ -350,12 +686,15 @@ int libconv_cnn_conv(int n, int nsys, int src_kind, int dst_kind, const void *sr
     if ((dst_kind == 0 && !bias) || (dst_kind == 1 && (!dst_fac || !bias)) || (dst_kind == 2 && !mask))
         return LIBCONV_EARG;
     cudaStream_t st = (cudaStream_t)stream;
+    int rc = LIBCONV_OK;
+    int *status = lcg::device_status(rc);
+    if (!status) return rc;
     cudaError_t e;
-    if (src_kind == 0 && dst_kind == 0) e = launch_conv<SRC_ACT, DST_ACT_RELU>(A, st);
-    else if (src_kind == 1 && dst_kind == 0) e = launch_conv<SRC_FIELD_EPS, DST_ACT_RELU>(A, st);
-    else if (src_kind == 0 && dst_kind == 1) e = launch_conv<SRC_ACT, DST_FIELD>(A, st);
-    else if (src_kind == 0 && dst_kind == 2) e = launch_conv<SRC_ACT, DST_ACT_MASK>(A, st);
-    else if (src_kind == 2 && dst_kind == 2) e = launch_conv<SRC_FIELD, DST_ACT_MASK>(A, st);
+    if (src_kind == 0 && dst_kind == 0) e = launch_conv<SRC_ACT, DST_ACT_RELU>(A, status, st);
+    else if (src_kind == 1 && dst_kind == 0) e = launch_conv<SRC_FIELD_EPS, DST_ACT_RELU>(A, status, st);
+    else if (src_kind == 0 && dst_kind == 1) e = launch_conv<SRC_ACT, DST_FIELD>(A, status, st);
+    else if (src_kind == 0 && dst_kind == 2) e = launch_conv<SRC_ACT, DST_ACT_MASK>(A, status, st);
+    else if (src_kind == 2 && dst_kind == 2) e = launch_conv<SRC_FIELD, DST_ACT_MASK>(A, status, st);
     else return LIBCONV_EARG;
     return e == cudaSuccess ? LIBCONV_OK : LIBCONV_ECUDA;
 }

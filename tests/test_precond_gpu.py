@@ -78,9 +78,10 @@ def test_conv_forward_field_and_relu(pkg, P):
     assert rel(out.float(), want) <= 1.6e-2
 
 
-def test_conv_field_input_with_eps_channel(pkg, P):
+@pytest.mark.parametrize('n', [8, 24])
+def test_conv_field_input_with_eps_channel(pkg, P, n):
     import torch
-    n, nsys = 8, 3
+    nsys = 3
     L = P._bind()
     g = torch.Generator().manual_seed(3)
     r = torch.randn(nsys * n ** 3, generator=g, dtype=torch.float64).cuda()
@@ -96,6 +97,54 @@ def test_conv_field_input_with_eps_channel(pkg, P):
                               P._p(out), None, None, 16, None, None) == 0
     torch.cuda.synchronize()
     assert rel(out.float().view(nsys, n, n, n, 16), ref) <= 1.6e-2
+
+
+@pytest.mark.parametrize('n', [24, 48])
+def test_conv_tensor_core_sizes_and_active(pkg, P, n):
+    """The tensor-core kernel (n >= 16; 8 x 16 x 4 tiles, the last y tile of
+    n = 24 overlapping the one before it) for every destination kind against
+    the FP32 reference; systems marked inactive are left untouched."""
+    import torch
+    nsys = 3
+    L = P._bind()
+    act = _rand_act(torch, nsys, n, 11)
+    W, wt = _rand_w(torch, 12)
+    bias = torch.linspace(-0.3, 0.4, 16).cuda()
+    ref = _conv_ref(act.float().permute(0, 4, 1, 2, 3), W, bias)
+    active = torch.tensor([1, 0, 1], dtype=torch.int32, device='cuda')
+    on = [0, 2]
+    out = torch.full_like(act, 7.0)
+    assert L.libconv_cnn_conv(n, nsys, 0, 0, P._p(act), None, None, P._p(wt), P._p(bias), P._p(out),
+                              None, None, 16, P._p(active), None) == 0
+    torch.cuda.synchronize()
+    want = torch.relu(ref).permute(0, 2, 3, 4, 1)
+    assert rel(out.float()[on], want[on]) <= 1.6e-2
+    assert bool((out[1].float() == 7.0).all())
+    fac = torch.tensor([0.5, 1.0, -2.0], dtype=torch.float64, device='cuda')
+    z = torch.zeros(nsys * n ** 3, dtype=torch.float64, device='cuda')
+    assert L.libconv_cnn_conv(n, nsys, 0, 1, P._p(act), None, None, P._p(wt), P._p(bias), P._p(z),
+                              P._p(fac), None, 1, None, None) == 0
+    torch.cuda.synchronize()
+    assert rel(z, (fac.view(-1, 1, 1, 1) * ref[:, 0].double()).reshape(-1)) <= 1e-4
+    # input-gradient kind: mask = a ReLU output
+    mask = torch.relu(act.float()).to(torch.bfloat16)
+    gin = torch.empty_like(act)
+    assert L.libconv_cnn_conv(n, nsys, 0, 2, P._p(act), None, None, P._p(wt), None, P._p(gin),
+                              None, P._p(mask), 16, None, None) == 0
+    torch.cuda.synchronize()
+    want = _conv_ref(act.float().permute(0, 4, 1, 2, 3), W).permute(0, 2, 3, 4, 1) * (mask.float() > 0)
+    assert rel(gin.float(), want) <= 1.6e-2
+    # single-channel field source with a mask (the last layer's input gradient)
+    r = torch.randn(nsys * n ** 3, dtype=torch.float64, device='cuda')
+    W1, wt1 = _rand_w(torch, 13, co=16, ci=1)
+    g1 = torch.empty_like(act)
+    assert L.libconv_cnn_conv(n, nsys, 2, 2, P._p(r), P._p(fac), None, P._p(wt1), None, P._p(g1),
+                              None, P._p(mask), 16, None, None) == 0
+    torch.cuda.synchronize()
+    x1 = _rnd((r.view(nsys, n, n, n) * fac.view(-1, 1, 1, 1)).float()).unsqueeze(1)
+    want = _conv_ref(x1, W1).permute(0, 2, 3, 4, 1) * (mask.float() > 0)
+    assert rel(g1.float(), want) <= 1.6e-2
+    assert L.libconv_gb300_check(None) == 0
 
 
 def test_input_and_weight_gradients(pkg, P):
