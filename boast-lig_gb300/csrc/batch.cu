@@ -37,6 +37,8 @@ struct Stage {
     long long units = 0;                     // tiles / blocks of the stage
     int grid = 0;                            // FP64 persistent grid
     TcFilter F;
+    int *d_lineE = nullptr;                  // exact tensor-core sweeps: line exponents of all grids
+    int exp_blocks = 0;                      // blocks per grid of their pass
 };
 
 struct OpConfig {
@@ -73,8 +75,10 @@ int fail_arg(const char *msg) { return report(LIBCONV_EARG, msg); }
 void free_stage(Stage &s) {
     if (s.d_desc) cudaFree(s.d_desc);
     if (s.d_prefix) cudaFree(s.d_prefix);
+    if (s.d_lineE) cudaFree(s.d_lineE);
     s.d_desc = nullptr;
     s.d_prefix = nullptr;
+    s.d_lineE = nullptr;
 }
 
 void drop_graph(libconv_batch *b) {
@@ -155,6 +159,23 @@ int configure(libconv_batch *b, int o, int engine, const int *ord) {
             if (sch == SCH_EXACT) tc_filter_digits(ftab + S0.ftab, S0.ntaps, a, st.F);
             else tc_filter_split(ftab + S0.ftab, S0.ntaps, a, sch, st.F);
             for (Sweep &S : st.sw) S.has_a = 0;   // folded into the filter operands
+            if (sch == SCH_EXACT) {
+                // one pre-pass per stage writes every line's largest exponent
+                long long lines = 0, most = 0;
+                bool contiguous = false;
+                for (Sweep &S : st.sw) {
+                    S.le_off = lines;
+                    const long long l = sweep_tc_lines(S);
+                    lines += l;
+                    most = l > most ? l : most;
+                    contiguous |= S.nL == 1;
+                }
+                st.exp_blocks = line_exp_batch_blocks(most, contiguous);
+                if (cudaMalloc(&st.d_lineE, sizeof(int) * (size_t)(lines > 0 ? lines : 1)) != cudaSuccess) {
+                    cudaGetLastError();
+                    return report(LIBCONV_ENOMEM, "batch line-exponent allocation failed");
+                }
+            }
         } else {
             st.grid = sweep_fp64_batch_grid(st.kind, st.ntaps, qc);
             if (st.grid <= 0) return report(LIBCONV_ECUDA, "no persistent grid for the FP64 sweep");
@@ -206,7 +227,7 @@ int launch_op(libconv_batch *b, int o, int *status, cudaStream_t stream) {
         cudaError_t e;
         if (C.engine == LIBCONV_ENGINE_TC)
             e = launch_sweep_tc_batch(st.kind, st.ntaps, st.d_desc, st.d_prefix, b->ngrids, st.F,
-                                      scheme_of(b->mode), status, stream);
+                                      scheme_of(b->mode), status, st.d_lineE, st.exp_blocks, stream);
         else
             e = launch_sweep_fp64_batch(st.kind, st.ntaps, C.engine == LIBCONV_ENGINE_FP64_Q32 ? 32 : 64,
                                         st.d_desc, st.d_prefix, b->ngrids, st.grid, stream);

@@ -30,6 +30,7 @@ struct Sweep {
     int has_a, has_ax, ay_mode, has_dot;   // ay_mode: 0 write, 1 a_y*y+out, 2 y+out
     double a, a_x, a_y;
     double *dot_part;         // one partial per block (device), when has_dot
+    long long le_off = 0;     // first entry of this sweep's lines in a batched line-exponent array
 };
 
 // Number of dot partials the FP64 sweep writes for S (grid size).

@@ -48,10 +48,16 @@ long long sweep_tc_lines(const Sweep &S);
 long long sweep_tc_tiles(const Sweep &S);
 bool sweep_tc_batch_supported(int kind, int ntaps);
 // One persistent launch over nsweeps sweeps (device descriptor array, tile
-// prefix sums with prefix[nsweeps] = total) of one kind and filter.
+// prefix sums with prefix[nsweeps] = total) of one kind and filter.  Exact
+// scheme with lineE: first one launch computes the largest exponent of every
+// line of every sweep into lineE (sweep i's lines from descs[i].le_off on,
+// exp_blocks blocks per sweep), so the sweeps read their input once.
 cudaError_t launch_sweep_tc_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
                                   int nsweeps, const TcFilter &F, int sch, int *status,
-                                  cudaStream_t st);
+                                  int *lineE, int exp_blocks, cudaStream_t st);
+// Blocks per sweep of the batched line-exponent pass for sweeps whose largest
+// line count (lines x narr) is max_lines, contiguous lines (nL == 1) or not.
+int line_exp_batch_blocks(long long max_lines, bool contiguous);
 
 namespace tck {
 long long tile_count_for(const Sweep &S, int qp);
@@ -68,7 +74,8 @@ cudaError_t launch_bf16x3(const Sweep &S, const TcFilter &F, int *status, const 
 cudaError_t launch_tf32x3(const Sweep &S, const TcFilter &F, int *status, const int *lineE,
                           cudaStream_t st);
 cudaError_t launch_exact_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
-                               int nsweeps, const TcFilter &F, int *status, cudaStream_t st);
+                               int nsweeps, const TcFilter &F, int *status, const int *lineE,
+                               cudaStream_t st);
 cudaError_t launch_bf16x3_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
                                 int nsweeps, const TcFilter &F, int *status, cudaStream_t st);
 cudaError_t launch_tf32x3_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,

@@ -36,7 +36,8 @@ long long tile_count_for(const Sweep &S, int qp) {
 // 0..plen-1 of every channel; ld padding is not read), one int per line of
 // every array.  Contiguous lines (nL == 1): a warp per line, lanes along the
 // line; strided lines: a thread per line, consecutive lines in a warp.
-__global__ void line_exp_kernel(const Sweep S, int plen, int *out) {
+__device__ __forceinline__ void line_exp_lines(const Sweep &S, int plen, int *out, long long first,
+                                               long long step) {
     const int nchan = S.kind == KCONV ? 1 : 2;
     const long long nlines = (long long)S.nL * S.nR, total = nlines * S.narr;
     const long long pext = (long long)S.in_ext * nchan;
@@ -48,8 +49,7 @@ __global__ void line_exp_kernel(const Sweep S, int plen, int *out) {
     const int count = plen * nchan;
     if (S.nL == 1) {
         const int lane = threadIdx.x & 31;
-        for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total;
-             w += ((long long)gridDim.x * blockDim.x) >> 5) {
+        for (long long w = first >> 5; w < total; w += step >> 5) {
             const long long arr = w / nlines, r = w % nlines;
             const long long *base = xb + arr * S.x_arr + pext * r;
             int mx = 0;
@@ -59,8 +59,7 @@ __global__ void line_exp_kernel(const Sweep S, int plen, int *out) {
             if (lane == 0) out[w] = mx;
         }
     } else {
-        for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-             t += (long long)gridDim.x * blockDim.x) {
+        for (long long t = first; t < total; t += step) {
             const long long arr = t / nlines, g = t % nlines;
             const long long l = g % S.nL, r = g / S.nL;
             const long long *base = xb + arr * S.x_arr + l + (long long)S.nL * pext * r;
@@ -70,6 +69,26 @@ __global__ void line_exp_kernel(const Sweep S, int plen, int *out) {
             out[t] = mx;
         }
     }
+}
+
+__global__ void line_exp_kernel(const Sweep S, int plen, int *out) {
+    line_exp_lines(S, plen, out, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+                   (long long)gridDim.x * blockDim.x);
+}
+
+// Input positions 0..plen-1 a sweep's outputs read along its line: the whole
+// line, or the used part of a shrink input.
+__host__ __device__ __forceinline__ int line_exp_plen(const Sweep &S) {
+    const int up = S.lowfil + S.ntaps - 1;
+    return S.bc == BC_SHRINK ? S.qhi + up - S.in_lo + 1 : S.n;
+}
+
+// The same maxima for a batch of sweeps: blockIdx.y = sweep, its lines'
+// maxima written from out + le_off on.
+__global__ void line_exp_batch_kernel(const Sweep *__restrict__ descs, int *out) {
+    const Sweep &S = descs[blockIdx.y];
+    line_exp_lines(S, line_exp_plen(S), out + S.le_off,
+                   (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
 }
 
 // Per-line exponent maxima of one n0 x n1 x n2 grid (narr of them, back to
@@ -217,10 +236,24 @@ bool sweep_tc_batch_supported(int kind, int ntaps) {
     return kind == KCONV && (ntaps == 16 || ntaps == 29);
 }
 
+int line_exp_batch_blocks(long long max_lines, bool contiguous) {
+    const long long threads = contiguous ? max_lines * 32 : max_lines;
+    const long long want = (threads + 255) / 256;
+    return (int)(want < 1 ? 1 : want > 64 ? 64 : want);
+}
+
 cudaError_t launch_sweep_tc_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
                                   int nsweeps, const TcFilter &F, int sch, int *status,
-                                  cudaStream_t st) {
-    if (sch == SCH_EXACT) return tck::launch_exact_batch(kind, ntaps, descs, prefix, nsweeps, F, status, st);
+                                  int *lineE, int exp_blocks, cudaStream_t st) {
+    if (sch == SCH_EXACT) {
+        if (lineE) {
+            if (exp_blocks < 1 || nsweeps > 65535) return cudaErrorInvalidValue;
+            tck::line_exp_batch_kernel<<<dim3(exp_blocks, nsweeps), 256, 0, st>>>(descs, lineE);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
+        return tck::launch_exact_batch(kind, ntaps, descs, prefix, nsweeps, F, status, lineE, st);
+    }
     if (sch == SCH_BF16X3) return tck::launch_bf16x3_batch(kind, ntaps, descs, prefix, nsweeps, F, status, st);
     if (sch == SCH_TF32X3) return tck::launch_tf32x3_batch(kind, ntaps, descs, prefix, nsweeps, F, status, st);
     return cudaErrorInvalidValue;
@@ -230,9 +263,7 @@ cudaError_t launch_sweep_tc(const Sweep &S, const TcFilter &F, int sch, int *sta
                             cudaStream_t st, bool lineE_ready) {
     if (sch == SCH_EXACT) {
         if (lineE && !lineE_ready) {
-            // positions a line's outputs read: 0..n-1, or the whole shrink input
-            const int up = S.lowfil + S.ntaps - 1;
-            const int plen = S.bc == BC_SHRINK ? S.qhi + up - S.in_lo + 1 : S.n;
+            const int plen = tck::line_exp_plen(S);
             const long long total = sweep_tc_lines(S);
             const long long threads = S.nL == 1 ? total * 32 : total;
             const long long want = (threads + 255) / 256;

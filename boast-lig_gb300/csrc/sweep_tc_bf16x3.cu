@@ -21,9 +21,9 @@ cudaError_t launch_bf16x3(const Sweep &S, const TcFilter &F, int *status, const 
 cudaError_t launch_bf16x3_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
                                int nsweeps, const TcFilter &F, int *status, cudaStream_t st) {
     if (kind == KCONV && ntaps == 16)
-        return launch_batch<KCONV, 16, SCH_BF16X3>(descs, prefix, nsweeps, F, status, st);
+        return launch_batch<KCONV, 16, SCH_BF16X3>(descs, prefix, nsweeps, F, status, nullptr, st);
     if (kind == KCONV && ntaps == 29)
-        return launch_batch<KCONV, 29, SCH_BF16X3>(descs, prefix, nsweeps, F, status, st);
+        return launch_batch<KCONV, 29, SCH_BF16X3>(descs, prefix, nsweeps, F, status, nullptr, st);
     return cudaErrorInvalidValue;
 }
 

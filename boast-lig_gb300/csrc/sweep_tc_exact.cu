@@ -19,11 +19,12 @@ cudaError_t launch_exact(const Sweep &S, const TcFilter &F, int *status, const i
 }
 
 cudaError_t launch_exact_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
-                               int nsweeps, const TcFilter &F, int *status, cudaStream_t st) {
+                               int nsweeps, const TcFilter &F, int *status, const int *lineE,
+                               cudaStream_t st) {
     if (kind == KCONV && ntaps == 16)
-        return launch_batch<KCONV, 16, SCH_EXACT>(descs, prefix, nsweeps, F, status, st);
+        return launch_batch<KCONV, 16, SCH_EXACT>(descs, prefix, nsweeps, F, status, lineE, st);
     if (kind == KCONV && ntaps == 29)
-        return launch_batch<KCONV, 29, SCH_EXACT>(descs, prefix, nsweeps, F, status, st);
+        return launch_batch<KCONV, 29, SCH_EXACT>(descs, prefix, nsweeps, F, status, lineE, st);
     return cudaErrorInvalidValue;
 }
 

@@ -552,7 +552,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             int mx = 0, E = 0;
             if (SCH == SCH_EXACT && lineE) {
                 // largest exponent field of the line (line_exp_kernel)
-                mx = valid ? lineE[(long long)arr * nlines + g] : 0;
+                mx = valid ? lineE[S.le_off + (long long)arr * nlines + g] : 0;
                 E = (mx ? mx : 1) - 1022;
             } else if (SCH == SCH_EXACT) {
 #pragma unroll
@@ -856,16 +856,17 @@ cudaError_t launch(const Sweep &S, const TcFilter &F, int *status, const int *li
 }
 
 // Batched launch over nsweeps descriptors (device arrays); S0 only carries
-// has_dot = 0.  One CTA per SM.
+// has_dot = 0.  One CTA per SM.  lineE (exact scheme, or null): line
+// exponent maxima of every sweep's lines, sweep i's at descs[i].le_off.
 template <int KIND, int NT, int SCH>
 cudaError_t launch_batch(const Sweep *descs, const long long *prefix, int nsweeps,
-                         const TcFilter &F, int *status, cudaStream_t st) {
+                         const TcFilter &F, int *status, const int *lineE, cudaStream_t st) {
     using G = Geom<KIND, NT, SCH>;
     cudaError_t e = set_smem_attr<KIND, NT, SCH, true>();
     if (e != cudaSuccess) return e;
     Sweep S0{};
     sweep_tc_kernel<KIND, NT, SCH, true><<<sm_count(), kThreads, G::SMEM, st>>>(S0, F, status, descs,
-                                                                                prefix, nsweeps, nullptr);
+                                                                                prefix, nsweeps, lineE);
     return cudaGetLastError();
 }
 
