@@ -429,7 +429,9 @@ int libconv_cg_apply(int n, int nsys, const double *h, const double *eps, const 
  * convergence (maxit + 1 if not reached); res (host, nsys or NULL): the
  * true residual norm ||b - (T - eps) x|| recomputed with the FP64 operator;
  * fell_back (host, nsys or NULL): the iteration at which a system left the
- * learned preconditioner for the plain one, 0 if it never did. */
+ * learned preconditioner for the plain one, 0 if it never did.  Returns
+ * LIBCONV_ETIMEOUT if a bounded device-side wait of its kinetic sweeps or
+ * network layers gave up (the device status word is read and cleared). */
 /* Stagnation test of the learned phase (calling thread): a system whose
  * residual norm is above ratio times its value `window` iterations earlier
  * (tested every `window` iterations) continues with the plain preconditioner
@@ -446,7 +448,9 @@ int libconv_cg_solve(int n, int nsys, const double *h, const double *eps, const 
  *          1: float64 field dst_fac[s] (conv channel 0 + bias[0]);
  *          2: bfloat16 activations conv, zeroed where mask (activations) <= 0.
  * cout: output channels computed (<= 8: channels 0-7 only); active (device,
- * nsys ints, or NULL): systems with 0 are skipped (their output untouched). */
+ * nsys ints, or NULL): systems with 0 are skipped (their output untouched).
+ * n >= 16 runs on the tensor cores (tcgen05); a bounded wait that gives up
+ * sets the device status word (libconv_gb300_check reports it). */
 int libconv_cnn_conv(int n, int nsys, int src_kind, int dst_kind, const void *src,
                      const double *src_fac, const double *eps, const void *wt, const float *bias,
                      void *dst, const double *dst_fac, const void *mask, int cout,
