@@ -95,62 +95,92 @@ __global__ void line_exp_batch_kernel(const Sweep *__restrict__ descs, int *out)
 // back) along all three axes in one read: e0[i1 + n1 (i2 + n2 a)] over i0,
 // e1[i0 + n0 (i2 + n2 a)] over i1, e2[i0 + n0 (i1 + n1 a)] over i2 -- the
 // line orders of the three non-rotating sweeps of the grid.  Block: 32 i0 x
-// 8 i1 threads, looping over i2 in chunks of 8 (8 loads in flight); e2 is a
-// thread's own maximum, e0 a warp maximum and e1 a block maximum, the last
-// two combined across blocks with atomicMax (e0, e1 zeroed first).
+// 8 i1 threads over one segment of i2 (blockIdx.z = a nseg + segment), in
+// chunks of 8 planes (8 loads in flight per thread).  e2 is a thread's own
+// maximum; each chunk is staged in shared memory (rows padded to 33 words,
+// so the row and the column reads below are free of bank conflicts), where
+// 4 threads per (plane, i1) row reduce the 32 i0 values for e0 and one
+// thread per (plane, i0) column the 8 i1 values for e1.  Partial maxima are
+// combined across blocks with atomicMax (e0, e1 and, with several segments,
+// e2 zeroed first).
 constexpr int kExpChunk = 8;
 __global__ void __launch_bounds__(256)
-line_exp3_kernel(const double *__restrict__ x, int n0, int n1, int n2, int *__restrict__ e0,
-                 int *__restrict__ e1, int *__restrict__ e2) {
-    __shared__ int ys[kExpChunk][8][32];
+line_exp3_kernel(const double *__restrict__ x, int n0, int n1, int n2, int nseg,
+                 int *__restrict__ e0, int *__restrict__ e1, int *__restrict__ e2) {
+    __shared__ int ys[kExpChunk][8][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int i0 = blockIdx.x * 32 + tx, i1 = blockIdx.y * 8 + ty;
-    const long long a = blockIdx.z;
+    const long long a = blockIdx.z / nseg;
+    const int seg = blockIdx.z % nseg, seglen = (n2 + nseg - 1) / nseg;
+    const int zb = seg * seglen, ze = min(n2, zb + seglen);
     const bool valid = i0 < n0 && i1 < n1;
     const long long plane = (long long)n0 * n1;
     const unsigned long long *xa =
         reinterpret_cast<const unsigned long long *>(x) + a * plane * n2 + i0 + (long long)n0 * i1;
+    // e1 reader: column (c1, tx) of the chunk; e0 reader: quarter q0 of row (c0r, r0)
+    const int c1 = ty, row = threadIdx.x >> 2, q0 = threadIdx.x & 3;
+    const int c0r = row >> 3, r0 = row & 7;
+    const int i1r = blockIdx.y * 8 + r0;
     int zmax = 0;
-    for (int c0 = 0; c0 < n2; c0 += kExpChunk) {
+    for (int c0 = zb; c0 < ze; c0 += kExpChunk) {
         int e[kExpChunk];
 #pragma unroll
         for (int c = 0; c < kExpChunk; ++c)
-            e[c] = (valid && c0 + c < n2) ? (int)((xa[plane * (c0 + c)] >> 52) & 0x7FF) : 0;
+            e[c] = (valid && c0 + c < ze) ? (int)((xa[plane * (c0 + c)] >> 52) & 0x7FF) : 0;
 #pragma unroll
         for (int c = 0; c < kExpChunk; ++c) {
             zmax = max(zmax, e[c]);
-            int w = e[c];
-            for (int o = 16; o > 0; o >>= 1) w = max(w, __shfl_xor_sync(0xffffffffu, w, o));
-            if (tx == 0 && i1 < n1 && c0 + c < n2)
-                atomicMax(e0 + i1 + (long long)n1 * (c0 + c + (long long)n2 * a), w);
             ys[c][ty][tx] = e[c];
         }
         __syncthreads();
-        if (ty == 0 && i0 < n0) {
-            for (int c = 0; c < kExpChunk && c0 + c < n2; ++c) {
-                int m = ys[c][0][tx];
+        if (c0 + c1 < ze && i0 < n0) {
+            int m = ys[c1][0][tx];
 #pragma unroll
-                for (int r = 1; r < 8; ++r) m = max(m, ys[c][r][tx]);
-                atomicMax(e1 + i0 + (long long)n0 * (c0 + c + (long long)n2 * a), m);
-            }
+            for (int r = 1; r < 8; ++r) m = max(m, ys[c1][r][tx]);
+            atomicMax(e1 + i0 + (long long)n0 * (c0 + c1 + (long long)n2 * a), m);
+        }
+        {
+            int m = ys[c0r][r0][8 * q0];
+#pragma unroll
+            for (int k = 1; k < 8; ++k) m = max(m, ys[c0r][r0][8 * q0 + k]);
+            m = max(m, __shfl_xor_sync(0xffffffffu, m, 1));
+            m = max(m, __shfl_xor_sync(0xffffffffu, m, 2));
+            if (q0 == 0 && c0 + c0r < ze && i1r < n1)
+                atomicMax(e0 + i1r + (long long)n1 * (c0 + c0r + (long long)n2 * a), m);
         }
         __syncthreads();
     }
-    if (valid) e2[i0 + (long long)n0 * (i1 + (long long)n1 * a)] = zmax;
+    if (valid) {
+        int *const p = e2 + i0 + (long long)n0 * (i1 + (long long)n1 * a);
+        if (nseg == 1) *p = zmax;
+        else atomicMax(p, zmax);
+    }
 }
 
 }  // namespace tck
+
+constexpr int kExpChunkHost = tck::kExpChunk;
 
 long long sweep_tc_lines(const Sweep &S) { return (long long)S.nL * S.nR * S.narr; }
 
 cudaError_t launch_line_exp3(const double *x, int n0, int n1, int n2, int narr, int *e0, int *e1,
                              int *e2, cudaStream_t st) {
     if (n0 < 1 || n1 < 1 || n2 < 1 || narr < 1 || narr > 65535) return cudaErrorInvalidValue;
+    const long long gx = (n0 + 31) / 32, gy = (n1 + 7) / 8;
+    // segments of i2 so that a few grids still give the GPU about 8 blocks per SM
+    const long long want = 8LL * tck::sm_count();
+    long long nseg = (want + gx * gy * narr - 1) / (gx * gy * narr);
+    const long long most = (n2 + kExpChunkHost - 1) / kExpChunkHost;
+    if (nseg > most) nseg = most;
+    if (nseg > 65535 / narr) nseg = 65535 / narr;
+    if (nseg < 1) nseg = 1;
     cudaError_t e = cudaMemsetAsync(e0, 0, (size_t)n1 * n2 * narr * sizeof(int), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(e1, 0, (size_t)n0 * n2 * narr * sizeof(int), st);
+    if (e == cudaSuccess && nseg > 1)
+        e = cudaMemsetAsync(e2, 0, (size_t)n0 * n1 * narr * sizeof(int), st);
     if (e != cudaSuccess) return e;
-    dim3 grid((unsigned)((n0 + 31) / 32), (unsigned)((n1 + 7) / 8), (unsigned)narr);
-    tck::line_exp3_kernel<<<grid, 256, 0, st>>>(x, n0, n1, n2, e0, e1, e2);
+    dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)(narr * nseg));
+    tck::line_exp3_kernel<<<grid, 256, 0, st>>>(x, n0, n1, n2, (int)nseg, e0, e1, e2);
     return cudaGetLastError();
 }
 

@@ -147,6 +147,32 @@ def test_conv_tensor_core_sizes_and_active(pkg, P, n):
     assert L.libconv_gb300_check(None) == 0
 
 
+def test_conv_tensor_core_many_tiles_per_cta(pkg, P):
+    """16 systems of 48^3: 1728 tiles over at most 3 CTAs per SM, so every CTA
+    runs several tiles (mbarrier phases alternating) and skips the tiles of
+    inactive systems between active ones."""
+    import torch
+    n, nsys = 48, 16
+    L = P._bind()
+    act = _rand_act(torch, nsys, n, 21)
+    W, wt = _rand_w(torch, 22)
+    bias = torch.linspace(-0.2, 0.3, 16).cuda()
+    active = torch.tensor([1, 1, 0, 1, 0, 0, 1, 1, 1, 0, 1, 1, 1, 1, 0, 1], dtype=torch.int32,
+                          device='cuda')
+    on = [s for s in range(nsys) if int(active[s]) != 0]
+    out = torch.full_like(act, -3.0)
+    assert L.libconv_cnn_conv(n, nsys, 0, 0, P._p(act), None, None, P._p(wt), P._p(bias), P._p(out),
+                              None, None, 16, P._p(active), None) == 0
+    torch.cuda.synchronize()
+    assert L.libconv_gb300_check(None) == 0
+    for s in range(nsys):
+        if s in on:
+            ref = _conv_ref(act[s:s + 1].float().permute(0, 4, 1, 2, 3), W, bias)
+            assert rel(out[s:s + 1].float(), torch.relu(ref).permute(0, 2, 3, 4, 1)) <= 1.6e-2, s
+        else:
+            assert bool((out[s].float() == -3.0).all()), s
+
+
 def test_input_and_weight_gradients(pkg, P):
     import torch
     n, nsys = 16, 2
