@@ -185,3 +185,67 @@ int main(int argc, char **argv) {
                          env={**os.environ, 'LD_LIBRARY_PATH': cuda_lib})
     assert run.returncode == 0, run.stderr
     assert run.stdout.split() == ['1', '0', '11', '12', '13']
+
+
+def _build_module():
+    import importlib.util
+    import os
+    import sys
+    here = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), 'boast-lig_gb300')
+    spec = importlib.util.spec_from_file_location('lcg_build_module', os.path.join(here, 'build.py'))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules['lcg_build_module'] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _prototypes(path, ret):
+    import re
+    text = re.sub(r'/\*.*?\*/', '', open(path).read(), flags=re.S)
+    return {n: ' '.join(a.split()).replace('* ', '*')
+            for n, a in re.findall(r'\b' + ret + r'\s+(\w+)\s*\(([^;{]*?)\)\s*;', text, flags=re.S)}
+
+
+def test_boast_void_shims(pkg, tmp_path):
+    """libconv_gb300_boast.so exports every procedure of include/libconv_boast.h
+    (the generated procedures' void prototypes), each declared with the same
+    parameters in libconv_gb300.h; the header is the one the build writes;
+    the main library binds its own entry points locally, so shims loaded
+    first cannot intercept its internal calls (the Fortran layer calls the C
+    entry points); a C caller built against the void prototypes links."""
+    import os
+    import shutil
+    import subprocess
+    B = _build_module()
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), 'include')
+    boast_h = os.path.join(inc, 'libconv_boast.h')
+    assert open(boast_h).read() == B.boast_header_text()
+    void_protos = _prototypes(boast_h, 'void')
+    int_protos = _prototypes(os.path.join(inc, 'libconv_gb300.h'), 'int')
+    assert len(void_protos) >= 20
+    for n, args in void_protos.items():
+        assert int_protos.get(n) == args, n
+    shim = os.path.join(os.path.dirname(pkg.LIB_PATH), 'libconv_gb300_boast.so')
+    assert os.path.exists(shim)
+    nm = subprocess.run(['nm', '-D', '--defined-only', shim], capture_output=True, text=True)
+    if nm.returncode == 0:
+        exported = {l.split()[2] for l in nm.stdout.splitlines() if ' T ' in l}
+        assert exported == set(void_protos), exported ^ set(void_protos)
+    re_out = subprocess.run(['readelf', '-rW', pkg.LIB_PATH], capture_output=True, text=True)
+    if re_out.returncode == 0:
+        for line in re_out.stdout.splitlines():
+            f = line.split()
+            assert not (len(f) >= 5 and f[4] in void_protos), line
+    cc = shutil.which('gcc')
+    if not cc:
+        pytest.skip('gcc missing')
+    src = tmp_path / 'boast_caller.c'
+    src.write_text('#include "libconv_boast.h"\n#include <stdio.h>\n'
+                   'int main(int argc, char **argv) {\n'
+                   '    if (argc > 5) d_s0s0_1d_sym8_md(0, 0, 0, 0, 0, 0, 0, 0, 0, 0.0, 0.0, 0.0);\n'
+                   '    if (argc > 5) d_kin(0, 0, 0, 0, 0, 0, 0, 0, 0.0, 0.0);\n'
+                   '    printf("linked\\n");\n    return 0;\n}\n')
+    exe = tmp_path / 'boast_caller'
+    r = subprocess.run([cc, '-I', inc, str(src), '-L', os.path.dirname(shim), '-l:libconv_gb300_boast.so',
+                        '-o', str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
