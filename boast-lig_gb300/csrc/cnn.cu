@@ -327,9 +327,12 @@ __global__ void reduce_parts(const float *part, int nparts, int len, float *out)
 // (cp.async for activations), thread 0 issues the MMAs and commits them to
 // an mbarrier, then warp w drains TMEM lanes 32 (w % 4) .. + 31 of half of
 // the output planes (bias + ReLU / mask / field scale, 32 B stored per
-// point).  Several CTAs reside per SM, so one CTA's staging overlaps
-// another's MMAs and epilogue.  Every wait is bounded; a wait that gives up
-// sets the device status word.
+// point).  Several CTAs reside per SM (three at TZ = 8), so one CTA's
+// staging overlaps another's MMAs and epilogue; on GB300 one M = 128 MMA of
+// this shape costs about 80 cycles whatever N (16-48), following its 4 KB A
+// tile, so the layer is bound by the number of A tiles read, which is what
+// the z-tap stacking cuts.  Every wait is bounded; a wait that gives up sets
+// the device status word.
 namespace tcc {
 constexpr int kTX = 8, kTY = 16;
 constexpr int kHX = kTX + 2, kHY = kTY + 2;
