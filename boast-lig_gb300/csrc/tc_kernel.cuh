@@ -38,15 +38,19 @@
 //   * one FP32 accumulator per output: relative error near 1e-7.
 //
 // Persistent, warp-specialised CTA (one per SM), 512 threads at <= 128
-// registers, one A buffer and two TMEM accumulator halves (output blocks 0-1
-// and 2-3 of a tile):
-//   warps 0-7  producers: thread = (row, half of the row segment); exact
-//              scheme: largest exponent of the row, then its byte digits;
-//              split schemes: bfloat16 / tf32 terms; coalesced or vector loads;
-//              warp 0 then issues the tile's MMAs (lane 0, fully unrolled,
-//              precomputed descriptors), each TMEM half as soon as the
-//              epilogue has released it;
-//   warps 8-15 epilogue: warps 8-11 drain TMEM half 0, warps 12-15 half 1;
+// registers, one A buffer used as a ring of three chunk pairs (input elements
+// [0, 32), [32, 64), [64, KT)) and two TMEM accumulator halves (output blocks
+// 0-1, which read pairs 0-1, and blocks 2-3, which read pairs 1-2):
+//   warps 0-7  producers: thread = (row, half of every pair); exact scheme:
+//              largest exponent of the row, then its byte digits; split
+//              schemes: bfloat16 / tf32 terms; coalesced or vector loads.  The
+//              pairs of a tile are written in order, pair 0 as soon as the
+//              previous tile's half-0 MMAs completed, pairs 1-2 once both
+//              halves' did, so the next tile's production overlaps the MMAs;
+//   warps 8-15 epilogue: group 0 (warps 8-11) owns TMEM half 0, group 1
+//              (12-15) half 1.  The group's first warp issues its half's MMAs
+//              (lane 0, fully unrolled, precomputed descriptors) once the
+//              pairs they read are written, then the group drains the half:
 //              thread = TMEM lane = tile row; TMEM -> FP64 -> global.
 // Every hand-off is an mbarrier whose phase can never run two phases ahead of
 // its waiter; every wait gives up after ~2 s of SM clock (status word set,
@@ -419,14 +423,19 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
     uint8_t *A = smem;
     uint8_t *B = smem + G::A_BYTES;
     uint8_t *aux = B + G::B_BYTES;
-    uint64_t *bars = (uint64_t *)aux;                 // 8 barriers
-    uint32_t *tslot = (uint32_t *)(aux + 64);
-    int *rowE = (int *)(aux + 1024);                  // producers -> MMA issuer
-    int *rowE_epi = rowE + kM;                        // MMA issuer -> epilogue, by tile parity
-    const uint32_t bA_full = saddr(&bars[0]), bA_empty = saddr(&bars[1]);
-    const uint32_t bT_full[2] = {saddr(&bars[2]), saddr(&bars[3])};
-    const uint32_t bT_empty[2] = {saddr(&bars[4]), saddr(&bars[5])};
-    const uint32_t bX_full[2] = {saddr(&bars[6]), saddr(&bars[7])};
+    uint64_t *bars = (uint64_t *)aux;                 // 9 barriers (16 slots)
+    uint32_t *tslot = (uint32_t *)(aux + 128);
+    int *rowE3 = (int *)(aux + 1024);                 // row exponents, by tile index mod 3
+    // pfull[p]: chunk pair p of the tile is written (producer arrivals);
+    // pfree0: pair 0 may be rewritten (the MMAs of TMEM half 0 completed);
+    // pfree12: pairs 1 and 2 may be rewritten (both halves' MMAs completed:
+    //          one commit from each issuer);
+    // bT_full[h]: TMEM half h holds the tile's accumulators;
+    // gsync[h]: the 4 warps of epilogue group h have drained TMEM half h.
+    const uint32_t pfull[3] = {saddr(&bars[0]), saddr(&bars[1]), saddr(&bars[2])};
+    const uint32_t pfree0 = saddr(&bars[3]), pfree12 = saddr(&bars[4]);
+    const uint32_t bT_full[2] = {saddr(&bars[5]), saddr(&bars[6])};
+    const uint32_t gsync[2] = {saddr(&bars[7]), saddr(&bars[8])};
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const long long ntiles = BATCH ? prefix[nsweeps]
@@ -442,12 +451,12 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (tid == 0) {
-        bar_init(bA_full, kProducers);
-        bar_init(bA_empty, 1);
+        for (int p = 0; p < 3; ++p) bar_init(pfull[p], kProducers);
+        bar_init(pfree0, 1);
+        bar_init(pfree12, 2);
         for (int h = 0; h < 2; ++h) {
             bar_init(bT_full[h], 1);
-            bar_init(bT_empty[h], 128);
-            bar_init(bX_full[h], 1);
+            bar_init(gsync[h], 128);
         }
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
@@ -474,14 +483,23 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
     const uint64_t b_desc0 = umma_desc(saddr(B), G::LBO_B, 128);
     if (warp < kProducers / 32) {
         // ============ producers: thread = (row, half of the row segment);
-        // half-warps cover 16 consecutive rows, lanes 0-15 elements [0, KT/2),
-        // lanes 16-31 [KT/2, KT).
-        constexpr int H = G::KT / 2;                                  // multiple of 8
+        // half-warps cover 16 consecutive rows.  The KT elements of a row are
+        // 8-element groups in three chunk pairs (elements [0, 32), [32, 64),
+        // [64, KT)); lanes 0-15 take the first half of every pair's groups,
+        // lanes 16-31 the second half, and both write the pairs in order, so
+        // pair 0 of the next tile (read only by the MMAs of TMEM half 0) is
+        // written while the MMAs of half 1 still read pairs 1 and 2.
+        constexpr int NG = G::KT / 8;                                 // 10 or 12 groups
+        constexpr int NGH = NG / 2;                                   // groups per thread
+        constexpr int G2 = (NG - 8) / 2;                              // per thread in pair 2
+        static_assert(NG == 10 || NG == 12, "three chunk pairs");
         const int half = lane >> 4;
         const int row = warp * 16 + (lane & 15);
+        auto group_of = [&](int c) -> int {          // c-th group of this thread
+            return c < 2 ? 2 * half + c : c < 4 ? 4 + 2 * half + (c - 2) : 8 + G2 * half + (c - 4);
+        };
         uint32_t it = 0;
         for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
-            if (it > 0 && !bar_wait(bA_empty, (it - 1) & 1)) { alive = false; break; }
             const TileLoc loc = locate<BATCH>(S0, descs, prefix, nsweeps, tile);
             const Sweep &S = *loc.S;
             const long long nlines = (long long)S.nL * S.nR;
@@ -518,33 +536,45 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             const long long l = valid ? g % S.nL : 0, r = valid ? g / S.nL : 0;
             const long long *base = xbits + (long long)arr * S.x_arr + l + (long long)S.nL * (in_ext * NCH) * r;
             const long long stride = S.nL;
-            const int k0 = half * H;
             const int klim = min(kneed, NCH * (plast - p0 + 1));
-            const int len = max(0, min(H, klim - k0));
-            const long long of0 = (valid && len > 0) ? off_of(k0) : -1;
-            const long long ofl = (valid && len > 0) ? off_of(k0 + len - 1) : -1;
-            // contiguous fast path: [k0, k0+len) is one unbroken 16-byte aligned run
-            const bool run = KIND != KREC && stride == 1 && of0 >= 0 && ofl == of0 + len - 1 &&
-                             ((((uintptr_t)(base + of0)) & 15) == 0);
-            auto load8 = [&](int c, long long (&bits)[8]) {
-                if (run) {
-                    const double2 *v = reinterpret_cast<const double2 *>(base + of0);
+            // contiguous fast path: the row's valid elements [0, klim) are one
+            // unbroken 16-byte aligned run (one check per row), or else the
+            // group's own valid elements are (a segment that wraps or starts
+            // outside a free line)
+            const bool lin = KIND != KREC && stride == 1 && valid && klim > 0;
+            const long long of0 = lin ? off_of(0) : -1;
+            const bool run_all = lin && of0 >= 0 && off_of(klim - 1) == of0 + klim - 1 &&
+                                 ((((uintptr_t)(base + of0)) & 15) == 0);
+            // the 8 elements of group gi
+            auto load8 = [&](int gi, long long (&bits)[8]) {
+                const int i0 = gi * 8;
+                const int cnt = max(0, min(8, klim - i0));
+                long long oa = -1, ob = -2;
+                if (run_all) {
+                    oa = of0 + i0;
+                    ob = oa + cnt - 1;
+                } else if (lin && cnt > 0) {
+                    oa = off_of(i0);
+                    ob = off_of(i0 + cnt - 1);
+                }
+                if (oa >= 0 && ob == oa + cnt - 1 && ((((uintptr_t)(base + oa)) & 15) == 0)) {
+                    const double2 *v = reinterpret_cast<const double2 *>(base + oa);
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
-                        const int i = c * 8 + 2 * e;
-                        if (i + 1 < len) {
-                            const double2 t = v[c * 4 + e];
+                        const int i = 2 * e;
+                        if (i + 1 < cnt) {
+                            const double2 t = v[e];
                             bits[2 * e] = __double_as_longlong(t.x);
                             bits[2 * e + 1] = __double_as_longlong(t.y);
                         } else {
-                            bits[2 * e] = i < len ? base[of0 + i] : 0ll;
+                            bits[2 * e] = i < cnt ? base[oa + i] : 0ll;
                             bits[2 * e + 1] = 0ll;
                         }
                     }
                 } else {
 #pragma unroll
                     for (int e = 0; e < 8; ++e) {
-                        const long long o = valid ? off_of(k0 + c * 8 + e) : -1;
+                        const long long o = valid ? off_of(i0 + e) : -1;
                         bits[e] = o >= 0 ? base[o * stride] : 0ll;
                     }
                 }
@@ -556,10 +586,10 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                 E = (mx ? mx : 1) - 1022;
             } else if (SCH == SCH_EXACT) {
 #pragma unroll
-                for (int c0 = 0; c0 < H / 8; c0 += 2) {          // 16 loads in flight
+                for (int c0 = 0; c0 < NGH; c0 += 2) {            // 16 loads in flight
                     long long b0[8], b1[8];
-                    load8(c0, b0);
-                    if (c0 + 1 < H / 8) load8(c0 + 1, b1);
+                    load8(group_of(c0), b0);
+                    if (c0 + 1 < NGH) load8(group_of(c0 + 1), b1);
                     else {
 #pragma unroll
                         for (int e = 0; e < 8; ++e) b1[e] = 0ll;
@@ -575,12 +605,19 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             // software pipeline: the next chunk's loads are in flight while the
             // current chunk is cut into digits
             long long bits[8], nxt[8];
-            load8(0, bits);
+            load8(group_of(0), bits);
+            bool ok = true;
 #pragma unroll 1
-            for (int c = 0; c < H / 8; ++c) {
-                if (c + 1 < H / 8) load8(c + 1, nxt);
+            for (int c = 0; c < NGH; ++c) {
+                if (c + 1 < NGH) load8(group_of(c + 1), nxt);
+                // pair 0 rewrites what the previous tile's TMEM-half-0 MMAs read,
+                // pairs 1 and 2 what both halves read
+                if (it > 0 && (c == 0 || c == 2) && !bar_wait(c == 0 ? pfree0 : pfree12, (it - 1) & 1)) {
+                    ok = false;
+                    break;
+                }
                 // 8 elements = 8 / CE core-matrix chunks of 2048 bytes (128 rows)
-                const int off = (half * (H / 8) + c) * (8 / G::CE) * 2048 + (row >> 3) * 128 + (row & 7) * 16;
+                const int off = group_of(c) * (8 / G::CE) * 2048 + (row >> 3) * 128 + (row & 7) * 16;
                 if (SCH == SCH_EXACT) {
                     uint32_t xl[8], xh[8], sg[8];
 #pragma unroll
@@ -623,35 +660,13 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                 }
 #pragma unroll
                 for (int e = 0; e < 8; ++e) bits[e] = nxt[e];
-            }
-            if (half == 0) rowE[row] = mx == 0x7FF ? 0x7FFFFFFF : E;
-            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-            bar_arrive(bA_full);
-            if (warp == 0) {
-                // ---- MMA issue for this tile, one TMEM half at a time
-                if (!bar_wait(bA_full, it & 1)) { alive = false; break; }
-                if (it > 0 && !bar_wait(bT_empty[0], (it - 1) & 1)) { alive = false; break; }
-#pragma unroll
-                for (int i = 0; i < kM / 32; ++i)
-                    rowE_epi[(it & 1) * kM + lane + 32 * i] = rowE[lane + 32 * i];
-                __syncwarp();
-                if (lane == 0) {
-                    bar_arrive(bX_full[0]);
-                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                    issue_half<KIND, NT, SCH, 0>(tmem, a_desc0, b_desc0);
-                    commit(bT_full[0]);
+                if (c == 1 || c == 3 || c == NGH - 1) {          // last group of a pair
+                    if (c == 1 && half == 0) rowE3[(it % 3) * kM + row] = mx == 0x7FF ? 0x7FFFFFFF : E;
+                    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                    bar_arrive(pfull[c == 1 ? 0 : c == 3 ? 1 : 2]);
                 }
-                __syncwarp();
-                if (it > 0 && !bar_wait(bT_empty[1], (it - 1) & 1)) { alive = false; break; }
-                if (lane == 0) {
-                    bar_arrive(bX_full[1]);
-                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                    issue_half<KIND, NT, SCH, 1>(tmem, a_desc0, b_desc0);
-                    commit(bT_full[1]);
-                    commit(bA_empty);
-                }
-                __syncwarp();
             }
+            if (!ok) { alive = false; break; }
         }
     } else {
         // ============ epilogue: warp group hf drains TMEM half hf (output blocks
@@ -671,10 +686,24 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
         };
         uint32_t it = 0;
         for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
-            if (!bar_wait(bX_full[hf], it & 1)) { alive = false; break; }
-            const int Er = rowE_epi[(it & 1) * kM + row];
+            // the group issues its TMEM half's MMAs for this tile (the half was
+            // drained by the group at the end of the previous tile) once the
+            // chunk pairs they read are written: half 0 pairs 0-1, half 1 pairs 1-2
+            if (!bar_wait(pfull[hf], it & 1) || !bar_wait(pfull[hf + 1], it & 1)) { alive = false; break; }
+            if (ew == 4 * hf) {
+                if (lane == 0) {
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    if (hf == 0) issue_half<KIND, NT, SCH, 0>(tmem, a_desc0, b_desc0);
+                    else issue_half<KIND, NT, SCH, 1>(tmem, a_desc0, b_desc0);
+                    commit(bT_full[hf]);
+                    if (hf == 0) commit(pfree0);
+                    commit(pfree12);
+                }
+                __syncwarp();
+            }
             if (!bar_wait(bT_full[hf], it & 1)) { alive = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const int Er = rowE3[(it % 3) * kM + row];
             const TileLoc loc = locate<BATCH>(S0, descs, prefix, nsweeps, tile);
             const Sweep &S = *loc.S;
             const long long nlines = (long long)S.nL * S.nR;
@@ -721,10 +750,6 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                                  (uint32_t)(hf * G::HALF_COLS + (jj * G::ORD + k) * 16 + n0),
                              acc[k]);
                 asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                if (step == 3) {                                // half drained: release it
-                    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-                    bar_arrive(bT_empty[hf]);
-                }
                 if (!valid) continue;
                 const int e0 = 16 * (2 * hf + jj) + n0;         // first output element of the step
                 const int q0 = qc0 + e0 / NCH;                  // e0 is a multiple of 8
@@ -814,6 +839,10 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                     }
                 }
             }
+            // the whole group has read TMEM half hf: it may be reissued
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            bar_arrive(gsync[hf]);
+            if (!bar_wait(gsync[hf], it & 1)) { alive = false; break; }
         }
         if (!BATCH && S0.has_dot && dot_arr >= 0) flush_dot();
     }
