@@ -1342,6 +1342,30 @@ def run_gpu(args):
             accuracy[name] = float((g - r).abs().max() / r.abs().max())
         pkg.set_mode(getattr(pkg, MODES[args.mode]))
 
+    # the configuration's second operator shape: free-BC grow MagicFilter3D on
+    # B grids of 64^3 (output 79^3), device-resident, timed on its own
+    grow = None
+    if W.name == 'mfkin128':
+        gn, gy = [64] * 3, [79] * 3
+        gx = torch.rand(B * 64 ** 3, dtype=torch.float64, device=dev) * 2 - 1
+        gyb = torch.empty(B * 79 ** 3, dtype=torch.float64, device=dev)
+        gw1, gw2 = torch.empty_like(gyb), torch.empty_like(gyb)
+        gk = pkg.Kernel('d_sfrf_ld_narr')
+        gop = lambda: gk.run_dev(3, gn, [1, 1, 1], gn, gy, B, gx, gyb, gw1, gw2, stream=sp)
+        for _ in range(3):
+            gop()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        for _ in range(10):
+            gop()
+        g1.record(stream)
+        g1.synchronize()
+        pkg.check(sp)
+        g_ms = g0.elapsed_time(g1) / 10
+        grow = {'op': 'MagicFilter3D free grow (d_sfrf_ld_narr, bc grow on every axis)',
+                'grids': B, 'in': '64^3', 'out': '79^3', 'ms': g_ms,
+                'in_pts_per_s': B * 64 ** 3 / (g_ms / 1e3), 'out_pts_per_s': B * 79 ** 3 / (g_ms / 1e3)}
+
     # e2e: the public host-pointer C-ABI with pinned host buffers, copies inside
     ho0 = torch.empty(B * max(Ni, No), dtype=torch.float64, pin_memory=True).numpy()
     ho1 = torch.empty(B * max(Ni, No), dtype=torch.float64, pin_memory=True).numpy()
@@ -1399,7 +1423,8 @@ def run_gpu(args):
             'config': {'workload': W.desc.format(B=B), 'grid': W.n, 'grids_per_gpu': B,
                        'mode': args.mode,
                        'l2': f'inputs larger than L2 ({B * Ni * 8 / 1e6:.0f} MB per array)',
-                       **{f'ms_{o}': t / args.steps for o, t in zip(W.ops, op_ms)}},
+                       **{f'ms_{o}': t / args.steps for o, t in zip(W.ops, op_ms)},
+                       **({'grow_magicfilter_64': grow} if grow else {})},
             'clocks': ck, 'e2e': e2e,
             # exact tensor-core sweeps are preceded by line-exponent passes
             'gpu_launches': args.steps * (W.launches + (W.exact_prepasses if args.mode == 'tc_exact'
