@@ -482,7 +482,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
     const uint64_t a_desc0 = umma_desc(saddr(A), 2048, 128);
     const uint64_t b_desc0 = umma_desc(saddr(B), G::LBO_B, 128);
     if (warp < kProducers / 32) {
-        // ============ producers: thread = (row, half of the row segment);
+        // ============ producers: thread = (row, half of every chunk pair);
         // half-warps cover 16 consecutive rows.  The KT elements of a row are
         // 8-element groups in three chunk pairs (elements [0, 32), [32, 64),
         // [64, KT)); lanes 0-15 take the first half of every pair's groups,
@@ -602,8 +602,8 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                 mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
                 E = (mx ? mx : 1) - 1022;
             }
-            // software pipeline: the next chunk's loads are in flight while the
-            // current chunk is cut into digits
+            // software pipeline: the next group's loads are in flight while the
+            // current group is cut into digits
             long long bits[8], nxt[8];
             load8(group_of(0), bits);
             bool ok = true;
@@ -669,8 +669,9 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             if (!ok) { alive = false; break; }
         }
     } else {
-        // ============ epilogue: warp group hf drains TMEM half hf (output blocks
-        // 2hf, 2hf+1); thread = TMEM lane = tile row; 8 outputs per step
+        // ============ epilogue: warp group hf issues and drains TMEM half hf
+        // (output blocks 2hf, 2hf+1); thread = TMEM lane = tile row; 8 outputs
+        // per step
         const int ew = warp - kProducers / 32;
         const int lq = ew & 3, hf = ew >> 2;
         const int row = lq * 32 + lane;
