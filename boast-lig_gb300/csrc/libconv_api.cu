@@ -1052,6 +1052,35 @@ int *device_status(int &rc) {
 }
 }  // namespace lcg
 
+namespace lcg {
+namespace {
+// Self-test of the bounded device waits: one thread waits on an mbarrier that
+// nothing arrives at, with the same try_wait / sleep / clock limit loop as the
+// tensor-core kernels, gives up after `limit` SM cycles and sets the status
+// word.  Nothing faults and the wait always ends.
+__global__ void selftest_wait_kernel(int *status, long long limit) {
+    __shared__ __align__(8) unsigned long long bar;
+    if (threadIdx.x != 0) return;
+    const uint32_t b = (uint32_t)__cvta_generic_to_shared(&bar);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(b) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    const long long t0 = clock64();
+    uint32_t ok = 0;
+    while (true) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(b)
+            : "memory");
+        if (ok || clock64() - t0 > limit) break;
+        __nanosleep(128);
+    }
+    if (!ok) atomicExch(status, 1);
+}
+}  // namespace
+}  // namespace lcg
+
 // =============================== exported C ABI ===============================
 extern "C" {
 
@@ -1082,6 +1111,21 @@ int libconv_gb300_check(void *stream) {
     cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "synchronize");
     return read_status(*s);
+}
+
+int libconv_gb300_selftest_wait(int wait_us, void *stream) {
+    if (wait_us < 1 || wait_us > 1000000) return fail(LIBCONV_EARG, "wait_us must be in [1, 1e6]");
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    int rc;
+    DevState *s = dev_state(rc);
+    if (!s) return rc;
+    int dev = 0, khz = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev) != cudaSuccess || khz <= 0) khz = 2000000;
+    lcg::selftest_wait_kernel<<<1, 32, 0, (cudaStream_t)stream>>>((int *)s->status.p,
+                                                                  (long long)wait_us * (khz / 1000));
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? LIBCONV_OK : cuda_fail(e, "self-test launch");
 }
 
 int libconv_gb300_set_mode(int mode) {

@@ -72,6 +72,11 @@ int libconv_gb300_get_mode(void);
  * device-side wait of an earlier *_dev call on this device gave up; clears
  * the device status word. */
 int libconv_gb300_check(void *stream);
+/* Self-test of the bounded device-side waits: enqueues on `stream` one wait on
+ * a barrier that nothing arrives at, limited to wait_us microseconds (1 to
+ * 1e6); it gives up, sets the device status word and returns, so the next
+ * libconv_gb300_check reports LIBCONV_ETIMEOUT (and clears the word). */
+int libconv_gb300_selftest_wait(int wait_us, void *stream);
 
 /* ---------------------------------------------------------------------
  * 1D sweeps: GenericConvolutionOperator1d#procedure
