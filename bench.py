@@ -186,6 +186,11 @@ class MfKin128:
         O.call('oracle_d_sfrf_ld_narr', 3, n, [0, 0, 0], n, n, 1, x, y, w1, w2)
         O.call('oracle_d_kin', 3, n, [0, 0, 0], x, tx, w1, w2, np.array(self.a), 0.0, 0.0)
 
+    def timing_step(self, T, O, B, x, o0, o1, threads):
+        """One step over B grids in the oracle's OpenMP timing build (seconds)."""
+        return T.timing_mfkin_step(B, O.ip(self.n), O.dp(x), O.dp(o0), O.dp(o1),
+                                   O.dp(np.array(self.a)), threads)
+
     # roofline: dominant kernel = the kinetic sweep (29 taps), 3 launches per
     # step over all grids; algorithmic bytes per grid point 64/3 per launch
     # (16 B first sweep, 24 B the two accumulating sweeps)
@@ -249,6 +254,9 @@ class Wavelet96:
         n = self.n
         O.call('oracle_d_idwt_sym8', 3, n, [0, 0, 0], x, y, w1, w2)
         O.call('oracle_d_dwt_sym8', 3, n, [0, 0, 0], y, back, w1, w2)
+
+    def timing_step(self, T, O, B, x, o0, o1, threads):
+        return T.timing_wavelet_step(B, O.ip(self.n), O.dp(x), O.dp(o0), O.dp(o1), threads)
 
     # roofline: every sweep moves 16 B per 96^3 point; dominant = the synthesis
     dom = 0
@@ -514,6 +522,82 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
+def fp64_peak(pkg, local):
+    """Measured FP64 FMA throughput of this GPU (libconv_gb300_fp64_peak: 8
+    independent FMA chains per thread, CUDA events), best of 3 launches of
+    about 0.4 s, with the SM clock sampled meanwhile."""
+    import ctypes
+    L = pkg.lib()
+    f = L.libconv_gb300_fp64_peak
+    f.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]
+    f.restype = ctypes.c_int
+    v = ctypes.c_double(0.0)
+    best = 0.0
+    ck = Clocks(local)
+    ck.start()
+    for _ in range(3):
+        if f(100000, ctypes.byref(v), None) != 0:
+            return None
+        best = max(best, v.value)
+    c = ck.stop()
+    return {'tflops': best, 'sm_mhz': c['sm_mhz'] if c else None,
+            'how': 'libconv_gb300_fp64_peak: 8 independent FMA chains x 100000 steps per thread, '
+                   '8 x SMs blocks of 256 threads, CUDA events, best of 3'}
+
+
+def cpu_model():
+    """CPU model name of this host (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(['lscpu'], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith('Model name:'):
+                return line.split(':', 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open('/proc/cpuinfo'):
+            if line.lower().startswith('model name'):
+                return line.split(':', 1)[1].strip()
+    except OSError:
+        pass
+    return 'unknown'
+
+
+def cpu_timed(W, B, hx, repeats=5, seconds=None):
+    """The oracle restatement's -O3 OpenMP timing build on the workload's own
+    batch: all host threads over the B grids of hx (one grid per thread at a
+    time), and one thread on one grid; each the minimum of at least `repeats`
+    timed runs after one untimed run, the reference's protocol
+    (GenericConvolution2.rb:1248-1252).  None when the timing build is
+    missing."""
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    T = O.timing_lib()
+    if T is None or not hasattr(W, 'timing_step'):
+        return None
+    th = cpu_threads()
+    N = max(W.n_in, W.n_out)
+    o0, o1 = np.zeros(B * N), np.zeros(B * N)
+    x = np.ascontiguousarray(hx[:B * W.n_in])
+    W.timing_step(T, O, B, x, o0, o1, th)
+    t_all = [W.timing_step(T, O, B, x, o0, o1, th) for _ in range(repeats)]
+    x1 = np.ascontiguousarray(hx[:W.n_in])
+    W.timing_step(T, O, 1, x1, o0, o1, 1)
+    t_one = [W.timing_step(T, O, 1, x1, o0, o1, 1) for _ in range(repeats)]
+    if min(t_all) <= 0 or min(t_one) <= 0:
+        return None
+    v_all, v_one = B * W.n_in / min(t_all), W.n_in / min(t_one)
+    return {'value': v_all, 'unit': UNIT, 'cores': th, 'kind': 'port',
+            'threads_all': {'threads': th, 'value': v_all, 'grids': B,
+                            'min_s': min(t_all), 'median_s': float(np.median(t_all))},
+            'threads_1': {'threads': 1, 'value': v_one, 'grids': 1, 'min_s': min(t_one),
+                          'median_s': float(np.median(t_one))},
+            'repeats': repeats, 'cpu_model': cpu_model(),
+            'build': 'oracle restatement, gcc -O3 -fopenmp (oracle/Makefile liblibconv_timing.so)',
+            'sample': f'the bench batch ({B} grids of the {W.name} operators) on {th} threads, and '
+                      f'one grid on 1 thread; min of {repeats} runs each after a warm-up run'}
+
+
 def cpu_baseline_sample(W, grids):
     """Bounded sample (~10 s): all host threads, one grid each, repeated."""
     th = cpu_threads()
@@ -669,6 +753,49 @@ def run_reference_poisson(args, W):
     print(json.dumps(line), flush=True)
 
 
+def reference_timed(args, W, grids, th):
+    """Reference arm on the GPU arm's own configuration: every step runs the
+    workload's operators over the same B grids (--grids) on all host threads
+    in the oracle's -O3 OpenMP timing build; value from the fastest step (the
+    reference's min-of-repeats protocol), the median beside it.  None when
+    the timing build is missing."""
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    T = O.timing_lib()
+    if T is None or not hasattr(W, 'timing_step'):
+        return None
+    B = args.grids
+    hx = np.zeros(B * W.n_in)
+    W.fill(hx, B, 0, grids)
+    N = max(W.n_in, W.n_out)
+    o0, o1 = np.zeros(B * N), np.zeros(B * N)
+    for _ in range(max(args.warmup, 1)):
+        W.timing_step(T, O, B, hx, o0, o1, th)
+    times = [W.timing_step(T, O, B, hx, o0, o1, th) for _ in range(args.steps)]
+    x1 = np.ascontiguousarray(hx[:W.n_in])
+    W.timing_step(T, O, 1, x1, o0, o1, 1)
+    t_one = [W.timing_step(T, O, 1, x1, o0, o1, 1) for _ in range(max(5, min(args.steps, 5)))]
+    t = min(times)
+    v = B * W.n_in / t
+    cb = {'value': v, 'unit': UNIT, 'cores': th, 'kind': 'port',
+          'threads_all': {'threads': th, 'value': v, 'grids': B, 'min_s': t,
+                          'median_s': float(np.median(times))},
+          'threads_1': {'threads': 1, 'value': W.n_in / min(t_one), 'grids': 1,
+                        'min_s': min(t_one), 'median_s': float(np.median(t_one))},
+          'repeats': args.steps, 'cpu_model': cpu_model(),
+          'build': 'oracle restatement, gcc -O3 -fopenmp (oracle/Makefile liblibconv_timing.so)',
+          'sample': f'{args.steps} steps of the {B}-grid batch on {th} threads (min), one grid '
+                    'on 1 thread'}
+    return {'impl': 'reference', 'metric': W.metric, 'value': v, 'unit': UNIT,
+            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': t * 1e3, 'ms_per_step_median': float(np.median(times)) * 1e3,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+            'data': 'synthetic (seeded)',
+            'config': {'workload': W.desc.format(B=B), 'grid': W.n, 'grids_per_gpu': B},
+            'cpu_baseline': cb,
+            'e2e': {'value': v, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+
+
 def run_reference(args):
     rank = int(os.environ.get('RANK', '0'))
     if rank != 0:
@@ -684,6 +811,10 @@ def run_reference(args):
         return run_reference_precond(args, W)
     grids = W.base(4)
     th = cpu_threads()
+    line = reference_timed(args, W, grids, th)
+    if line:
+        print(json.dumps(line), flush=True)
+        return
     times, pts = cpu_run(W, grids, th, args.steps, max(args.warmup, 1))
     t = float(np.median(times))
     v = pts / t
@@ -848,10 +979,11 @@ def run_orbitals(args, W):
         line['cpu_baseline'] = {'value': pts / t, 'unit': UNIT, 'cores': th, 'kind': 'port',
                                 'sample': f'{pts / 1e6:.1f} M orbital points in {t:.1f} s, '
                                           'C oracle, orbitals round robin over host threads'}
-    if rank == 0:
+    if rank == 0 and getattr(args, 'emit', True):
         print(json.dumps(line), flush=True)
     B.close()
     R.close()
+    return line
 
 
 def run_precond(args, W):
@@ -976,9 +1108,10 @@ def run_precond(args, W):
         line['cpu_baseline'] = {'value': k / t, 'unit': 'solves/s', 'cores': th, 'kind': 'port',
                                 'sample': f'{k} plain-CG solves in {t:.1f} s (C oracle kinetic), '
                                           'one system per host thread at a time'}
-    if rank == 0:
+    if rank == 0 and getattr(args, 'emit', True):
         print(json.dumps(line), flush=True)
     R.close()
+    return line
 
 
 def run_hamiltonian(args, W):
@@ -1410,10 +1543,16 @@ def run_gpu(args):
                                'note': f'{prods} operand-plane products, K={W.kb} per 16 outputs'
                                        + ('; tf32 peak = half the measured bf16 peak'
                                           if args.mode == 'tc_tf32x3' else '')}
-    else:
-        roof['fp64_pipe'] = {'achieved_tflops': W.dom_flops_per_pt * pts_launch / t_launch / 1e12,
-                             'nominal_peak_tflops': 1.25,
+    fp = fp64_peak(pkg, local) if getattr(args, 'emit', True) else None
+    if args.mode == 'fp64':
+        ach = W.dom_flops_per_pt * pts_launch / t_launch / 1e12
+        roof['fp64_pipe'] = {'achieved_tflops': ach,
+                             'peak_tflops': fp['tflops'] if fp else None,
+                             'frac': ach / fp['tflops'] if fp else None,
+                             'peak_source': 'measured' if fp else None, 'peak': fp,
                              'note': 'plain FP64 FMA path: bound by the FP64 pipe, not HBM'}
+    elif fp:
+        roof['fp64_pipe_peak'] = fp
     exact = args.mode in ('fp64', 'tc_exact')
     line = {'metric': W.metric, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
             'warmup': max(args.warmup, 3), 'ms_per_step': ms / args.steps, 'higher_is_better': True,
@@ -1433,10 +1572,82 @@ def run_gpu(args):
     if accuracy:
         line['accuracy_max_rel_error'] = accuracy
     if rank == 0 and world == 1 and not args.no_cpu:
-        line['cpu_baseline'] = cpu_baseline_sample(W, base)
-    if rank == 0:
+        line['cpu_baseline'] = cpu_timed(W, B, hx) or cpu_baseline_sample(W, base)
+    if W.name == 'mfkin128' and world == 1 and getattr(args, 'emit', True) and not args.no_sub:
+        # free the headline buffers first: the sub-records allocate their own
+        del bufs, ops
+        torch.cuda.empty_cache()
+        line['config'].update(sub_records(args))
+    if rank == 0 and getattr(args, 'emit', True):
         print(json.dumps(line), flush=True)
     R.close()
+    return line
+
+
+def sub_records(args):
+    """The other configurations of the metric, measured in the same run after
+    the headline (one GPU, each bounded to a few steps): the 96^3 wavelet
+    round trip (throughput in the exact mode, and the split-precision
+    schemes' max relative error per operator), the 512 uneven orbitals
+    (batched graph throughput and the tuner's choice) and the 256 learned-
+    preconditioner solves (learned and plain CG solves/s, their ratio and the
+    largest true FP64 residual).  A failure is recorded, not raised."""
+    import argparse as _ap
+    out = {}
+
+    def sub(workload, mode, steps):
+        a = _ap.Namespace(**vars(args))
+        a.workload, a.mode, a.steps, a.warmup = workload, mode, steps, 3
+        a.no_cpu, a.emit, a.no_sub, a.grids = True, False, True, 32
+        W = WORKLOADS[workload]
+        if workload == 'orbitals512':
+            return run_orbitals(a, W)
+        if workload == 'precond256':
+            return run_precond(a, W)
+        return run_gpu(a)
+
+    try:
+        t0 = time.perf_counter()
+        wl = sub('wavelet96', 'tc_exact', 5)
+        rec = {'workload': wl['config']['workload'], 'gpts_per_s': wl['value'] / 1e9,
+               'e2e_gpts_per_s': wl['e2e']['value'] / 1e9, 'ms_idwt3d': wl['config']['ms_idwt3d'],
+               'ms_dwt3d': wl['config']['ms_dwt3d'], 'mode': 'tc_exact'}
+        for m in ('tc_bf16x3', 'tc_tf32x3'):
+            ws = sub('wavelet96', m, 2)
+            rec[m] = {'gpts_per_s': ws['value'] / 1e9,
+                      'max_rel_error': {k: v for k, v in ws['accuracy_max_rel_error'].items()
+                                        if k != 'reference'}}
+        rec['seconds'] = time.perf_counter() - t0
+        out['wavelet96'] = rec
+    except Exception as e:   # noqa: BLE001 -- recorded in the line
+        out['wavelet96'] = {'error': repr(e)[:300]}
+    try:
+        t0 = time.perf_counter()
+        ob = sub('orbitals512', 'tc_exact', 5)
+        c = ob['config']
+        out['orbitals512'] = {'workload': c['workload'], 'gpts_per_s': ob['value'] / 1e9,
+                              'e2e_gpts_per_s': ob['e2e']['value'] / 1e9, 'tuned': c['tuned'],
+                              'tune_seconds': c['tune_seconds'],
+                              'batched_speedup_vs_per_grid_calls': c['batched_speedup_vs_per_grid_calls'],
+                              'mode': 'tc_exact', 'seconds': time.perf_counter() - t0}
+    except Exception as e:   # noqa: BLE001
+        out['orbitals512'] = {'error': repr(e)[:300]}
+    try:
+        t0 = time.perf_counter()
+        pc = sub('precond256', 'tc_exact', 3)
+        c = pc['config']
+        out['precond256'] = {'workload': c['workload'], 'learned_solves_per_s': pc['value'],
+                             'plain_cg_solves_per_s': c['plain_cg_solves_per_s'],
+                             'learned_over_plain': c['learned_over_plain'],
+                             'max_true_residual': c['max_true_residual'],
+                             'plain_cg_max_true_residual': c['plain_cg_max_true_residual'],
+                             'iterations_mean': c['iterations_mean'],
+                             'plain_cg_iterations_mean': c['plain_cg_iterations_mean'],
+                             'e2e_solves_per_s': pc['e2e']['value'],
+                             'tolerance': 1e-8, 'seconds': time.perf_counter() - t0}
+    except Exception as e:   # noqa: BLE001
+        out['precond256'] = {'error': repr(e)[:300]}
+    return out
 
 
 def main():
@@ -1450,6 +1661,9 @@ def main():
     ap.add_argument('--systems', type=int, default=None,
                     help='precond256: number of systems (default 256; smaller for profiling)')
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline sample')
+    ap.add_argument('--no-sub', action='store_true',
+                    help='mfkin128: skip the other configurations (wavelet96, orbitals512, '
+                         'precond256) recorded under config after the headline')
     ap.add_argument('--no-tune', action='store_true',
                     help='orbitals512: use the cached or default batch configuration')
     ap.add_argument('--mode', default='tc_exact', choices=list(MODES),

@@ -29,6 +29,7 @@
 
 #include "../../include/libconv_gb300.h"
 #include "lcg_plan.cuh"
+#include "lcg_pool.cuh"
 #include "libconv_filters.h"
 
 namespace {
@@ -257,23 +258,35 @@ __global__ void k_norms(const double *part, double *out, int nsys) {
 }
 
 // ---- workspace -------------------------------------------------------------------
-struct Work {
-    void *p = nullptr;
-    size_t cap = 0;
-};
+// Per device, a pool of workspaces leased per call (lcg_pool.cuh): an apply
+// only enqueues on the caller's stream, so calls on different streams get
+// different workspaces.
 std::mutex g_mu;
-Work g_work[64];
+lcg::StreamPool g_pool[64];
 
-int ensure(Work &w, size_t bytes) {
-    if (w.cap >= bytes) return LIBCONV_OK;
-    if (w.p) cudaFree(w.p);
-    w.p = nullptr;
-    w.cap = 0;
-    if (cudaMalloc(&w.p, bytes) != cudaSuccess) {
+struct WorkLease {
+    lcg::StreamPool *pool = nullptr;
+    lcg::PoolEntry *e = nullptr;
+    cudaStream_t st = nullptr;
+    WorkLease() = default;
+    WorkLease(const WorkLease &) = delete;
+    WorkLease &operator=(const WorkLease &) = delete;
+    ~WorkLease() { if (pool && e) pool->release(e, st); }
+    void *p() const { return e->p[0]; }
+};
+
+int lease(WorkLease &w, size_t bytes, cudaStream_t st) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+        return lcg::report(LIBCONV_ECUDA, "no current device");
+    const cudaError_t e = g_pool[dev].acquire(st, &bytes, 1, w.e);
+    if (e != cudaSuccess) {
         cudaGetLastError();
-        return lcg::report(LIBCONV_ENOMEM, "CG workspace allocation failed");
+        return lcg::report(e == cudaErrorMemoryAllocation ? LIBCONV_ENOMEM : LIBCONV_ECUDA,
+                           "CG workspace allocation failed");
     }
-    w.cap = bytes;
+    w.pool = &g_pool[dev];
+    w.st = st;
     return LIBCONV_OK;
 }
 
@@ -322,13 +335,11 @@ int libconv_cg_apply(int n, int nsys, const double *h, const double *eps, const 
     if (n < 1 || nsys < 1 || !h || !eps || !x || !y) return lcg::report(LIBCONV_EARG, "bad CG apply arguments");
     const long long N = (long long)n * n * n;
     std::lock_guard<std::mutex> lk(g_mu);
-    int dev = 0;
-    cudaGetDevice(&dev);
-    Work &w = g_work[dev & 63];
     const size_t need = sizeof(double) * (3 * N * nsys + (size_t)kBPS * nsys);
-    int rc = ensure(w, need);
+    WorkLease w;
+    int rc = lease(w, need, (cudaStream_t)stream);
     if (rc) return rc;
-    double *w1 = (double *)w.p, *w2 = w1 + N * nsys, *Tx = w2 + N * nsys, *part = Tx + N * nsys;
+    double *w1 = (double *)w.p(), *w2 = w1 + N * nsys, *Tx = w2 + N * nsys, *part = Tx + N * nsys;
     const double a[3] = {-0.5 / (h[0] * h[0]), -0.5 / (h[1] * h[1]), -0.5 / (h[2] * h[2])};
     return apply_A(n, nsys, a, eps, x, y, w1, w2, Tx, part, (cudaStream_t)stream);
 }
@@ -341,9 +352,6 @@ int libconv_cg_solve(int n, int nsys, const double *h, const double *eps, const 
     cudaStream_t st = (cudaStream_t)stream;
     const long long N = (long long)n * n * n, SN = N * nsys;
     std::lock_guard<std::mutex> lk(g_mu);
-    int dev = 0;
-    cudaGetDevice(&dev);
-    Work &w = g_work[dev & 63];
     // r, p, Ap, z, Tp, w1, w2 (FP64 vectors); two 16-channel BF16 activations;
     // partial sums; scalars
     const size_t vec = sizeof(double) * SN, act = sizeof(__nv_bfloat16) * 16 * SN;
@@ -351,9 +359,10 @@ int libconv_cg_solve(int n, int nsys, const double *h, const double *eps, const 
     // 15 sub-buffers, each rounded up to 256 bytes
     const size_t need = 7 * vec + 2 * act + 5 * parts + sizeof(double) * 10 * nsys +
                         sizeof(int) * 3 * nsys + 17 * 256;
-    int rc = ensure(w, need);
+    WorkLease w;
+    int rc = lease(w, need, st);
     if (rc) return rc;
-    uint8_t *q = (uint8_t *)w.p;
+    uint8_t *q = (uint8_t *)w.p();
     auto take = [&](size_t bytes) { uint8_t *r = q; q += (bytes + 255) & ~(size_t)255; return r; };
     double *r = (double *)take(vec), *p = (double *)take(vec), *Ap = (double *)take(vec),
            *z = (double *)take(vec), *Tp = (double *)take(vec), *w1 = (double *)take(vec),

@@ -15,6 +15,7 @@
 
 #include "../../include/libconv_gb300.h"
 #include "lcg_plan.cuh"
+#include "lcg_pool.cuh"
 #include "lcg_sweep.cuh"
 #include "lcg_tc.cuh"
 #include "libconv_filters.h"
@@ -124,8 +125,9 @@ struct DevState {
     PipeSlot pipe[kPipeSlots];       // chunked host-pointer execution (exec_host)
     cudaStream_t stream = nullptr;   // stream of the host-pointer entry points
     DevBuf buf[6];                   // x, y, w1, w2, dot partials, dot scalar
-    DevBuf scratch;                  // dot partials of the *_dev entry points
-    DevBuf lineexp;                  // per-line exponents of the exact tensor-core sweeps
+    DevBuf scratch;                  // dot partials of the host-pointer entry points
+    DevBuf lineexp;                  // their per-line exponents (exact tensor-core sweeps)
+    StreamPool pool;                 // scratch of the *_dev entry points, per call (lcg_pool.cuh)
     DevBuf dscalar;
     DevBuf status;                   // device status word (bounded waits)
     DevBuf potpart;                  // partial sums of the potential energy
@@ -378,11 +380,64 @@ int plan_kin(int d, const int *n, const int *bc, const double *a, double a_x, do
 }
 
 // ---- execution ------------------------------------------------------------------
+// Device scratch one plan run uses: dot partials (doubles) and per-line
+// exponents of the exact tensor-core sweeps (ints), sized by plan_scratch
+// before anything is enqueued.
+struct Scratch {
+    double *dot = nullptr;
+    size_t ndot = 0;
+    int *le = nullptr;
+    size_t nle = 0;
+};
+
+// Elements of dot partials and of line exponents that run_plan(P) needs in
+// the calling thread's mode.
+void plan_scratch(const Plan &P, size_t &ndot, size_t &nle) {
+    ndot = nle = 0;
+    const bool exact = t_mode == LIBCONV_MODE_TC_EXACT;
+    if (exact && P.exp3[0] > 0) {
+        const size_t n0 = P.exp3[0], n1 = P.exp3[1], n2 = P.exp3[2], na = P.exp3[3];
+        nle = (n1 * n2 + n0 * n2 + n0 * n1) * na;
+    }
+    for (const PlanStep &ps : P.steps) {
+        const Sweep &S = ps.S;
+        const bool tc = t_mode != LIBCONV_MODE_FP64 && sweep_tc_supported(S);
+        if (S.has_dot) {
+            const size_t nb = tc ? (size_t)sweep_tc_blocks(S) * 8 * S.narr : (size_t)sweep_fp64_blocks(S);
+            if (nb > ndot) ndot = nb;
+        }
+        const bool shared = exact && P.exp3[0] > 0 && ps.exp_axis >= 0 && ps.src == B_X;
+        if (tc && exact && !shared && (size_t)sweep_tc_lines(S) > nle) nle = (size_t)sweep_tc_lines(S);
+    }
+}
+
+// The host-pointer paths' scratch: their own buffers, grown under the lock
+// (the host call synchronises before it returns).
+int host_scratch(const Plan &P, DevBuf &dot, DevBuf &le, Scratch &sc) {
+    size_t nd, nl;
+    plan_scratch(P, nd, nl);
+    int rc;
+    if (nd && (rc = ensure(dot, nd * sizeof(double)))) return rc;
+    if (nl && (rc = ensure(le, nl * sizeof(int)))) return rc;
+    sc.dot = (double *)dot.p;
+    sc.ndot = dot.cap / sizeof(double);
+    sc.le = (int *)le.p;
+    sc.nle = le.cap / sizeof(int);
+    return LIBCONV_OK;
+}
+
 // Launch the plan's sweeps with bound device pointers.  dot_dev receives the
-// dot product (device) when the plan has one; `scratch` holds the partials.
-int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, DevBuf &lineexp,
-             double *dot_dev, int *status, cudaStream_t st) {
+// dot product (device) when the plan has one; the partials and line
+// exponents live in sc (at least plan_scratch's sizes).
+int run_plan(const Plan &P, double *const bufs[4], const Scratch &sc, double *dot_dev, int *status,
+             cudaStream_t st) {
     if (!valid_mode(t_mode)) return fail(LIBCONV_EMODE, "unknown mode %d", t_mode);
+    {
+        size_t nd, nl;
+        plan_scratch(P, nd, nl);
+        if (nd > sc.ndot || nl > sc.nle || (nd && !sc.dot) || (nl && !sc.le))
+            return fail(LIBCONV_EARG, "internal: plan scratch not sized");
+    }
     // exact tensor-core sweeps of one grid along its three axes: the line
     // exponents of all three come from one read of x
     int *shared_exp = nullptr;
@@ -391,9 +446,7 @@ int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, DevBuf &line
         const long long n0 = P.exp3[0], n1 = P.exp3[1], n2 = P.exp3[2], na = P.exp3[3];
         exp_off[1] = n1 * n2 * na;
         exp_off[2] = exp_off[1] + n0 * n2 * na;
-        int rc = ensure(lineexp, (size_t)(exp_off[2] + n0 * n1 * na) * sizeof(int));
-        if (rc) return rc;
-        shared_exp = (int *)lineexp.p;
+        shared_exp = sc.le;
         cudaError_t e = launch_line_exp3(bufs[B_X], (int)n0, (int)n1, (int)n2, (int)na, shared_exp,
                                          shared_exp + exp_off[1], shared_exp + exp_off[2], st);
         if (e != cudaSuccess) return cuda_fail(e, "line exponent launch");
@@ -415,9 +468,7 @@ int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, DevBuf &line
                 nb = sweep_fp64_blocks(S);
                 seg = nb / S.narr;
             }
-            int rc = ensure(scratch, (size_t)nb * sizeof(double));
-            if (rc) return rc;
-            S.dot_part = (double *)scratch.p;
+            S.dot_part = sc.dot;
             if (tc && S.narr > 1) {   // slots of arrays a CTA has no tile of stay 0
                 cudaError_t e = cudaMemsetAsync(S.dot_part, 0, (size_t)nb * sizeof(double), st);
                 if (e != cudaSuccess) return cuda_fail(e, "clear dot partials");
@@ -439,9 +490,7 @@ int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, DevBuf &line
                 lineE = shared_exp + exp_off[ps.exp_axis];
             } else if (sch == SCH_EXACT) {
                 if (shared_exp) return fail(LIBCONV_EARG, "plan shares line exponents but a step does not");
-                int rc = ensure(lineexp, (size_t)sweep_tc_lines(S) * sizeof(int));
-                if (rc) return rc;
-                lineE = (int *)lineexp.p;
+                lineE = sc.le;
             }
             e = launch_sweep_tc(S, F, sch, status, lineE, st, shared);
         } else {
@@ -459,6 +508,41 @@ int run_plan(const Plan &P, double *const bufs[4], DevBuf &scratch, DevBuf &line
     return LIBCONV_OK;
 }
 
+// A pool entry of the current device for one enqueue-only call on st: buffer
+// 0 dot partials, 1 line exponents, 2 potential-energy partials (bytes).
+// Released by ~Lease after the call's work is enqueued.  Caller holds g_mu.
+struct Lease {
+    DevState *s = nullptr;
+    PoolEntry *e = nullptr;
+    cudaStream_t st = nullptr;
+    Lease() = default;
+    Lease(const Lease &) = delete;
+    Lease &operator=(const Lease &) = delete;
+    ~Lease() { if (s && e) s->pool.release(e, st); }
+    int take(DevState *ds, cudaStream_t stream, size_t dot_b, size_t le_b, size_t pot_b = 0) {
+        const size_t bytes[3] = {dot_b, le_b, pot_b};
+        cudaError_t err = ds->pool.acquire(stream, bytes, 3, e);
+        if (err != cudaSuccess) {
+            cudaGetLastError();
+            return err == cudaErrorMemoryAllocation
+                       ? fail(LIBCONV_ENOMEM, "scratch allocation (%zu + %zu + %zu bytes): %s", dot_b,
+                              le_b, pot_b, cudaGetErrorString(err))
+                       : cuda_fail(err, "scratch lease");
+        }
+        s = ds;
+        st = stream;
+        return LIBCONV_OK;
+    }
+    Scratch scratch() const {
+        Scratch sc;
+        sc.dot = (double *)e->p[0];
+        sc.ndot = e->cap[0] / sizeof(double);
+        sc.le = (int *)e->p[1];
+        sc.nle = e->cap[1] / sizeof(int);
+        return sc;
+    }
+};
+
 // Device-pointer execution (caller-owned buffers, no host synchronisation).
 int exec_dev(const Plan &P, const double *x, double *y, double *w1, double *w2, double *dot_dev,
              void *stream) {
@@ -471,7 +555,11 @@ int exec_dev(const Plan &P, const double *x, double *y, double *w1, double *w2, 
     int rc;
     DevState *s = dev_state(rc);
     if (!s) return rc;
-    return run_plan(P, bufs, s->scratch, s->lineexp, dot_dev, (int *)s->status.p, (cudaStream_t)stream);
+    size_t nd, nl;
+    plan_scratch(P, nd, nl);
+    Lease L;
+    if ((rc = L.take(s, (cudaStream_t)stream, nd * sizeof(double), nl * sizeof(int)))) return rc;
+    return run_plan(P, bufs, L.scratch(), dot_dev, (int *)s->status.p, (cudaStream_t)stream);
 }
 
 // Read and clear the device status word (after the work was synchronised).
@@ -541,6 +629,8 @@ int exec_host_pipelined(const Plan &P, int narr, const double *x, double *y, Dev
         }
         for (int b = 0; b < 4; ++b)
             if (Qc.elems[b] && (rc = ensure(ps.buf[b], Qc.elems[b] * sizeof(double)))) return rc;
+        Scratch unused;   // sized for the full chunk (the last chunk needs no more)
+        if ((rc = host_scratch(Qc, ps.scratch, ps.lineexp, unused))) return rc;
     }
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < nchunk && e == cudaSuccess; ++k) {
@@ -555,8 +645,9 @@ int exec_host_pipelined(const Plan &P, int narr, const double *x, double *y, Dev
             e = cudaMemcpyAsync(bufs[B_Y], y + a0 * ys, ca * ys * sizeof(double),
                                 cudaMemcpyHostToDevice, ps.stream);
         if (e != cudaSuccess) break;
-        if ((rc = run_plan(Q, bufs, ps.scratch, ps.lineexp, nullptr, (int *)s.status.p, ps.stream)))
-            return rc;
+        Scratch sc;
+        if ((rc = host_scratch(Q, ps.scratch, ps.lineexp, sc))) return rc;
+        if ((rc = run_plan(Q, bufs, sc, nullptr, (int *)s.status.p, ps.stream))) return rc;
         e = cudaMemcpyAsync(y + a0 * ys, bufs[B_Y], ca * ys * sizeof(double), cudaMemcpyDeviceToHost,
                             ps.stream);
     }
@@ -593,8 +684,9 @@ int exec_host(const Plan &P, const double *x, double *y, double *dot_host) {
         e = cudaMemcpyAsync(bufs[B_Y], y, P.y_read * sizeof(double), cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) return cuda_fail(e, "copy y to device");
     }
-    rc = run_plan(P, bufs, s->scratch, s->lineexp, P.has_dot ? (double *)s->dscalar.p : nullptr,
-                  (int *)s->status.p, st);
+    Scratch sc;
+    if ((rc = host_scratch(P, s->scratch, s->lineexp, sc))) return rc;
+    rc = run_plan(P, bufs, sc, P.has_dot ? (double *)s->dscalar.p : nullptr, (int *)s->status.p, st);
     if (rc) return rc;
     e = cudaMemcpyAsync(y, bufs[B_Y], P.elems[B_Y] * sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e != cudaSuccess) return cuda_fail(e, "copy y to host");
@@ -660,30 +752,57 @@ int plan_ham(const int *n, const int *bc, const double *a_kin, int norb, Ham &H)
     return LIBCONV_OK;
 }
 
+// Scratch of one run_ham: the largest need of its five plans, and the
+// potential-energy partials (doubles).
+void ham_scratch(const Ham &H, size_t &ndot, size_t &nle, size_t &npot) {
+    ndot = nle = 0;
+    for (const Plan *P : {&H.idwt, &H.mf, &H.imf, &H.kin, &H.dwt}) {
+        size_t a, b;
+        plan_scratch(*P, a, b);
+        if (a > ndot) ndot = a;
+        if (b > nle) nle = b;
+    }
+    npot = (size_t)potential_blocks((long long)H.nreal) * (size_t)H.norb;
+}
+
 // Enqueue the pipeline on `st`.  work: H.nwork() doubles; energies: 4
-// doubles per orbital (ekin of the three directions, then epot), device.
+// doubles per orbital (ekin of the three directions, then epot), device;
+// sc and potpart at least ham_scratch's sizes.
 int run_ham(const Ham &H, const double *psig, const double *pot, double *rho, double *hpsig,
-            double *work, double *energies, DevState &s, cudaStream_t st) {
+            double *work, double *energies, const Scratch &sc, double *potpart, int *status,
+            cudaStream_t st) {
     const size_t no = (size_t)H.norb;
     double *fscf = work, *hpsi = fscf + no * H.nfscf, *psir = hpsi + no * H.nfscf;
     double *w1 = psir + no * H.nreal, *w2 = w1 + H.nw;
-    int *status = (int *)s.status.p;
     double *b_idwt[4] = {const_cast<double *>(psig), fscf, w1, w2};
-    int rc = run_plan(H.idwt, b_idwt, s.scratch, s.lineexp, nullptr, status, st);
+    int rc = run_plan(H.idwt, b_idwt, sc, nullptr, status, st);
     if (rc) return rc;
     double *b_mf[4] = {fscf, psir, w1, w2};
-    if ((rc = run_plan(H.mf, b_mf, s.scratch, s.lineexp, nullptr, status, st))) return rc;
-    const long long nb = potential_blocks((long long)H.nreal);
-    if ((rc = ensure(s.potpart, (size_t)nb * no * sizeof(double)))) return rc;
-    cudaError_t e = launch_potential(psir, pot, rho, (long long)H.nreal, H.norb,
-                                     (double *)s.potpart.p, energies + 3, 4, st);
+    if ((rc = run_plan(H.mf, b_mf, sc, nullptr, status, st))) return rc;
+    cudaError_t e = launch_potential(psir, pot, rho, (long long)H.nreal, H.norb, potpart,
+                                     energies + 3, 4, st);
     if (e != cudaSuccess) return cuda_fail(e, "potential launch");
     double *b_imf[4] = {psir, hpsi, w1, w2};
-    if ((rc = run_plan(H.imf, b_imf, s.scratch, s.lineexp, nullptr, status, st))) return rc;
+    if ((rc = run_plan(H.imf, b_imf, sc, nullptr, status, st))) return rc;
     double *b_kin[4] = {fscf, hpsi, w1, w2};
-    if ((rc = run_plan(H.kin, b_kin, s.scratch, s.lineexp, energies, status, st))) return rc;
+    if ((rc = run_plan(H.kin, b_kin, sc, energies, status, st))) return rc;
     double *b_dwt[4] = {hpsi, hpsig, w1, w2};
-    return run_plan(H.dwt, b_dwt, s.scratch, s.lineexp, nullptr, status, st);
+    return run_plan(H.dwt, b_dwt, sc, nullptr, status, st);
+}
+
+// The host-pointer Hamiltonian's scratch: the library's own buffers.
+int ham_host_scratch(const Ham &H, DevState &s, Scratch &sc) {
+    size_t nd, nl, np;
+    ham_scratch(H, nd, nl, np);
+    int rc;
+    if (nd && (rc = ensure(s.scratch, nd * sizeof(double)))) return rc;
+    if (nl && (rc = ensure(s.lineexp, nl * sizeof(int)))) return rc;
+    if ((rc = ensure(s.potpart, np * sizeof(double)))) return rc;
+    sc.dot = (double *)s.scratch.p;
+    sc.ndot = s.scratch.cap / sizeof(double);
+    sc.le = (int *)s.lineexp.p;
+    sc.nle = s.lineexp.cap / sizeof(int);
+    return LIBCONV_OK;
 }
 
 // Host-pointer form over many orbitals: chunks of orbitals pipelined on three
@@ -702,6 +821,8 @@ int ham_host_pipelined(const Ham &H, const int *n, const int *bc, const double *
     const size_t ns = H.nsig, nc = (size_t)c * ns;
     const size_t nd = (rho ? 2 : 1) * H.nreal + Hc.nwork() + 4 * nc + 4 * (size_t)norb;
     if ((rc = ensure(s.hbuf, nd * sizeof(double)))) return rc;
+    Scratch sc;   // one compute stream: the chunks use it in turn
+    if ((rc = ham_host_scratch(Hc, s, sc))) return rc;
     double *d_pot = (double *)s.hbuf.p, *d_rho = rho ? d_pot + H.nreal : nullptr;
     double *d_work = d_pot + (rho ? 2 : 1) * H.nreal;
     double *d_in[2] = {d_work + Hc.nwork(), d_work + Hc.nwork() + nc};
@@ -739,7 +860,8 @@ int ham_host_pipelined(const Ham &H, const int *n, const int *bc, const double *
         if (e == cudaSuccess) e = cudaStreamWaitEvent(scomp, ev_in[k], 0);
         if (e == cudaSuccess && k >= 2) e = cudaStreamWaitEvent(scomp, ev_out[k - 2], 0);
         if (e != cudaSuccess) break;
-        rc = run_ham(Q, d_in[b], d_pot, d_rho, d_out[b], d_work, d_en + 4 * a0, s, scomp);
+        rc = run_ham(Q, d_in[b], d_pot, d_rho, d_out[b], d_work, d_en + 4 * a0, sc, (double *)s.potpart.p,
+                     (int *)s.status.p, scomp);
         if (rc) break;
         e = cudaEventRecord(ev_done[k], scomp);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(sout, ev_done[k], 0);
@@ -789,7 +911,11 @@ int ham_host(const Ham &H, const double *psig, const double *pot, double *rho, d
     if (e == cudaSuccess && rho)
         e = cudaMemcpyAsync(d_rho, rho, H.nreal * sizeof(double), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(e, "copy inputs to device");
-    if ((rc = run_ham(H, d_psig, d_pot, d_rho, d_hpsig, d_work, d_en, *s, st))) return rc;
+    Scratch sc;
+    if ((rc = ham_host_scratch(H, *s, sc))) return rc;
+    if ((rc = run_ham(H, d_psig, d_pot, d_rho, d_hpsig, d_work, d_en, sc, (double *)s->potpart.p,
+                      (int *)s->status.p, st)))
+        return rc;
     e = cudaMemcpyAsync(hpsig, d_hpsig, ns * sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess && rho)
         e = cudaMemcpyAsync(rho, d_rho, H.nreal * sizeof(double), cudaMemcpyDeviceToHost, st);
@@ -1002,7 +1128,11 @@ int poisson_sweep(int nord, int idim, const int *nn, int bc, double a, bool accu
     DevState *s = dev_state(rc);
     if (!s) return rc;
     double *bufs[4] = {const_cast<double *>(x), y, nullptr, nullptr};
-    if ((rc = run_plan(P, bufs, s->scratch, s->lineexp, nullptr, (int *)s->status.p, st))) return rc;
+    size_t nd, nl;
+    plan_scratch(P, nd, nl);
+    Lease L;
+    if ((rc = L.take(s, st, nd * sizeof(double), nl * sizeof(int)))) return rc;
+    if ((rc = run_plan(P, bufs, L.scratch(), nullptr, (int *)s->status.p, st))) return rc;
     if (nper) {
         cudaError_t e = launch_poisson_edges(x, y, nL, n, nR, nord, a, accumulate ? 1 : 0, st);
         if (e != cudaSuccess) return cuda_fail(e, "Poisson boundary launch");
@@ -1054,17 +1184,24 @@ int *device_status(int &rc) {
 
 namespace lcg {
 namespace {
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // Self-test of the bounded device waits: one thread waits on an mbarrier that
-// nothing arrives at, with the same try_wait / sleep / clock limit loop as the
-// tensor-core kernels, gives up after `limit` SM cycles and sets the status
-// word.  Nothing faults and the wait always ends.
-__global__ void selftest_wait_kernel(int *status, long long limit) {
+// nothing arrives at, with the same try_wait / sleep / limit loop as the
+// tensor-core kernels, gives up after `limit_ns` nanoseconds of the GPU's
+// global timer (independent of the SM clock) and sets the status word.
+// Nothing faults and the wait always ends.
+__global__ void selftest_wait_kernel(int *status, unsigned long long limit_ns) {
     __shared__ __align__(8) unsigned long long bar;
     if (threadIdx.x != 0) return;
     const uint32_t b = (uint32_t)__cvta_generic_to_shared(&bar);
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(b) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    const long long t0 = clock64();
+    const unsigned long long t0 = global_ns();
     uint32_t ok = 0;
     while (true) {
         asm volatile(
@@ -1073,10 +1210,29 @@ __global__ void selftest_wait_kernel(int *status, long long limit) {
             : "=r"(ok)
             : "r"(b)
             : "memory");
-        if (ok || clock64() - t0 > limit) break;
+        if (ok || global_ns() - t0 > limit_ns) break;
         __nanosleep(128);
     }
     if (!ok) atomicExch(status, 1);
+}
+
+// FP64 pipe probe: every thread runs 8 independent FMA chains (no dependency
+// between consecutive FMAs of a chain's neighbours), so the FP64 pipe, not
+// latency, bounds the kernel.  The sink store happens only for a value the
+// chains never reach, which keeps the compiler from removing them.
+__device__ double g_fp64_sink;
+__global__ void __launch_bounds__(256) fp64_peak_kernel(int iters, double a, double b) {
+    double v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = (double)(threadIdx.x + j);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = fma(v[j], a, b);
+    }
+    double t = 0.0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) t += v[j];
+    if (t == -1.0) g_fp64_sink = t;
 }
 }  // namespace
 }  // namespace lcg
@@ -1119,13 +1275,40 @@ int libconv_gb300_selftest_wait(int wait_us, void *stream) {
     int rc;
     DevState *s = dev_state(rc);
     if (!s) return rc;
-    int dev = 0, khz = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev) != cudaSuccess || khz <= 0) khz = 2000000;
     lcg::selftest_wait_kernel<<<1, 32, 0, (cudaStream_t)stream>>>((int *)s->status.p,
-                                                                  (long long)wait_us * (khz / 1000));
+                                                                  1000ull * (unsigned long long)wait_us);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? LIBCONV_OK : cuda_fail(e, "self-test launch");
+}
+
+int libconv_gb300_fp64_peak(int iters, double *tflops, void *stream) {
+    if (iters < 1 || iters > (1 << 24) || !tflops) return fail(LIBCONV_EARG, "iters in [1, 2^24], tflops not null");
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_fail(e, "device query");
+    const int grid = 8 * sms;          // 8 blocks of 256 threads per SM
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess) {
+        lcg::fp64_peak_kernel<<<grid, 256, 0, st>>>(iters / 8 + 1, 1.0000001, 1e-9);   // warm-up
+        e = cudaEventRecord(e0, st);
+        if (e == cudaSuccess) lcg::fp64_peak_kernel<<<grid, 256, 0, st>>>(iters, 1.0000001, 1e-9);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cuda_fail(e, "FP64 peak probe");
+    const double flops = 2.0 * 8.0 * (double)iters * (double)grid * 256.0;
+    *tflops = ms > 0.0f ? flops / (ms * 1e-3) / 1e12 : 0.0;
+    return LIBCONV_OK;
 }
 
 int libconv_gb300_set_mode(int mode) {
@@ -1358,7 +1541,14 @@ int libconv_hamiltonian_narr_dev(const int *n, const int *bc, const double *a_ki
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     DevState *s = dev_state(rc);
     if (!s) return rc;
-    return run_ham(H, psig, pot, rho, hpsig, work, energies, *s, (cudaStream_t)stream);
+    size_t nd, nl, np;
+    ham_scratch(H, nd, nl, np);
+    Lease L;
+    if ((rc = L.take(s, (cudaStream_t)stream, nd * sizeof(double), nl * sizeof(int),
+                     np * sizeof(double))))
+        return rc;
+    return run_ham(H, psig, pot, rho, hpsig, work, energies, L.scratch(), (double *)L.e->p[2],
+                   (int *)s->status.p, (cudaStream_t)stream);
 }
 
 int d_s0s0_1d_sym8_md_cost(int d, int idim, const int *n, int bc, int narr, long long *cost) {

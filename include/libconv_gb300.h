@@ -23,6 +23,16 @@
  * The *_dev entry points take DEVICE pointers and a cudaStream_t (passed as
  * void*, NULL = legacy default stream); they only enqueue work, and a
  * dot_in output of a *_dev entry point is a device pointer.
+ *
+ * Streams: the scratch a *_dev call needs besides the caller's buffers (dot
+ * partial sums, per-line exponents of the exact tensor-core sweeps, energy
+ * partials, the CG apply workspace) is leased to that call alone from a
+ * per-device pool: calls on different streams, from one thread or several,
+ * may be in flight at the same time and never share scratch (when more than
+ * 16 streams are in flight at once, a new call is ordered after the oldest).
+ * Calls on one stream reuse one lease in stream order.  The only state the
+ * calls share is the device status word of the bounded waits (an error
+ * flag) and, for d_s0s0_1d_sym8_d2_dotin_noalloc alone, its fixed array.
  */
 #ifndef LIBCONV_GB300_H
 #define LIBCONV_GB300_H
@@ -74,9 +84,16 @@ int libconv_gb300_get_mode(void);
 int libconv_gb300_check(void *stream);
 /* Self-test of the bounded device-side waits: enqueues on `stream` one wait on
  * a barrier that nothing arrives at, limited to wait_us microseconds (1 to
- * 1e6); it gives up, sets the device status word and returns, so the next
- * libconv_gb300_check reports LIBCONV_ETIMEOUT (and clears the word). */
+ * 1e6) of the GPU's global timer; it gives up, sets the device status word
+ * and returns, so the next libconv_gb300_check reports LIBCONV_ETIMEOUT (and
+ * clears the word).  (The kernels' own waits give up after 4e9 SM clock
+ * cycles, about 2 s at the maximum clock, longer at lower clocks.) */
 int libconv_gb300_selftest_wait(int wait_us, void *stream);
+/* Diagnostic, no counterpart in the reference: measured FP64 FMA throughput
+ * of this GPU (the roof of the plain FP64 sweeps).  Runs 8 independent FMA
+ * chains of `iters` steps in 8 x SMs blocks of 256 threads on `stream`, times
+ * the launch with CUDA events and synchronises; *tflops = 2 x FMAs / time. */
+int libconv_gb300_fp64_peak(int iters, double *tflops, void *stream);
 
 /* ---------------------------------------------------------------------
  * 1D sweeps: GenericConvolutionOperator1d#procedure
@@ -157,9 +174,11 @@ int d_s0s1_1d_symicomb8_dev(int d, int idim, const int *n, int bc, const int *nx
  * ceil(outputs / 64), times narr) is rejected with LIBCONV_ESIZE.
  * The first call on a device looks up that array's device address (a CUDA
  * runtime query, done once per device, with the device current); make the
- * first call before any stream capture.  Calls share the array: calls that
- * overlap on the GPU (different streams, concurrently) race.  Always runs the
- * FP64 sweep kernel, whatever the compute mode. */
+ * first call before any stream capture; cudaDeviceReset between calls is not
+ * supported (the address looked up before it would be stale).  Calls share
+ * the array: calls that overlap on the GPU (different streams, concurrently)
+ * race, and what they corrupt is dot_in (y does not use the array).  Always
+ * runs the FP64 sweep kernel, whatever the compute mode. */
 int d_s0s0_1d_sym8_d2_dotin_noalloc(int d, int idim, const int *n, int bc, const int *nx,
                                     const int *ny, int narr, const double *x, double *y,
                                     double a, double a_x, double a_y, double *dot_in,

@@ -58,11 +58,15 @@ _SIGS['oracle_update_rhopol'] = [_int, _int, _int, _int, _D, _int, _D, _dbl, _D,
 _SIGS['oracle_div_u_i_ref'] = [_int, _int, _int, _int, _D, _D, _int, _D]
 
 
-def build(ref=None):
-    """Compile the oracle (and the reference MagicFilter.c when the reference
-    tree is mounted).  Returns True when the reference build was made."""
+def build(ref=None, ref_dir=None):
+    """Compile the oracle, and the reference's MagicFilter.c when the
+    reference tree is given (ref_dir, else $LIBCONV_REFERENCE_DIR; no default:
+    without it the reference build is skipped).  Returns True when the
+    reference build was made."""
     subprocess.run(['make', '-s', '-C', HERE, 'all'], check=True)
-    ref_dir = os.environ.get('LIBCONV_REFERENCE_DIR', '/root/reference')
+    ref_dir = ref_dir or os.environ.get('LIBCONV_REFERENCE_DIR')
+    if not ref_dir:
+        return False
     want_ref = ref if ref is not None else os.path.isdir(ref_dir)
     if want_ref and os.path.isfile(os.path.join(ref_dir, 'benchmark/convolutions-c/MagicFilter.c')):
         subprocess.run(['make', '-s', '-C', HERE, 'ref', f'REF_DIR={ref_dir}'], check=True)
@@ -83,6 +87,28 @@ def lib():
             fn.restype = None if name.endswith(('_per_ref', '_per_t_ref', '_free_ref', '_free_t_ref', '_ref_ekin')) or name == 'oracle_kinetic_per_ref' else ctypes.c_int
         _LIB = L
     return _LIB
+
+
+_TIMING = None
+
+
+def timing_lib():
+    """The CPU baseline timing build (liblibconv_timing.so: the restatement at
+    -O3 with OpenMP step drivers), or None when it is not built."""
+    global _TIMING
+    if _TIMING is None:
+        path = os.path.join(HERE, 'liblibconv_timing.so')
+        if not os.path.exists(path):
+            return None
+        T = ctypes.CDLL(path)
+        T.timing_mfkin_step.argtypes = [_int, _I, _D, _D, _D, _D, _int]
+        T.timing_mfkin_step.restype = ctypes.c_double
+        T.timing_wavelet_step.argtypes = [_int, _I, _D, _D, _D, _int]
+        T.timing_wavelet_step.restype = ctypes.c_double
+        T.timing_max_threads.argtypes = []
+        T.timing_max_threads.restype = _int
+        _TIMING = T
+    return _TIMING
 
 
 def ref_lib():

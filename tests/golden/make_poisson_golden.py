@@ -11,7 +11,9 @@ poisson_fd_c1d.npz as float64 arrays fd<nord>[j + m, i] = c1D(i - m, j), so
 the library's own table can be checked against the reference's bits on
 machines without the reference tree.
 
-    python tests/golden/make_poisson_golden.py [path/to/BigDFT/Poisson.rb]
+    python tests/golden/make_poisson_golden.py path/to/BigDFT/Poisson.rb
+
+(or with $LIBCONV_REFERENCE_DIR set to the reference tree).
 """
 import os
 import re
@@ -20,7 +22,6 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT = '/root/reference/BigDFT/Poisson.rb'
 
 
 def literal(tok):
@@ -52,7 +53,13 @@ def parse(text):
 
 
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else DEFAULT
+    if len(sys.argv) > 1:
+        src = sys.argv[1]
+    elif os.environ.get('LIBCONV_REFERENCE_DIR'):
+        src = os.path.join(os.environ['LIBCONV_REFERENCE_DIR'], 'BigDFT', 'Poisson.rb')
+    else:
+        sys.exit('usage: make_poisson_golden.py path/to/BigDFT/Poisson.rb '
+                 '(or set LIBCONV_REFERENCE_DIR)')
     tables = parse(open(src).read())
     assert sorted(tables) == ['fd16', 'fd2', 'fd4', 'fd6', 'fd8'], sorted(tables)
     np.savez(os.path.join(HERE, 'poisson_fd_c1d.npz'), **tables)

@@ -59,7 +59,13 @@ def test_magicfilter_grow_ld_narr9(pkg):
     k.run(3, n, [1, 1, 1], nx, ny, narr, pinned(x), yh, np.zeros(1), np.zeros(1))
     w = np.zeros(narr * M * 2)
     yd, = dev_run(k, [3, n, [1, 1, 1], nx, ny, narr, x, y0.copy(), w, w.copy()], [7])
-    assert np.array_equal(yh, yd)
+    # the computed region; the ld padding lines of the output are computed from
+    # the padding of the intermediate workspaces (the caller's zeros here, the
+    # library's staging for the host call), as the generated loops do
+    Yh, Yd = yh.reshape(narr, ny[2], ny[1], ny[0]), yd.reshape(narr, ny[2], ny[1], ny[0])
+    q = [v + 15 for v in n]
+    sl = (slice(None), slice(0, q[2]), slice(0, q[1]), slice(0, q[0]))
+    assert np.array_equal(Yh[sl], Yd[sl])
 
 
 def test_kinetic_narr_with_ay(pkg):
