@@ -158,7 +158,10 @@ int configure(libconv_batch *b, int o, int engine, const int *ord) {
             const double a = S0.has_a ? S0.a : 1.0;
             if (sch == SCH_EXACT) tc_filter_digits(ftab + S0.ftab, S0.ntaps, a, st.F);
             else tc_filter_split(ftab + S0.ftab, S0.ntaps, a, sch, st.F);
-            for (Sweep &S : st.sw) S.has_a = 0;   // folded into the filter operands
+            for (Sweep &S : st.sw) {
+                S.has_a = 0;   // folded into the filter operands
+                if (!tc_prepare(S)) return report(LIBCONV_EARG, "batch grid too large for the tensor-core sweep");
+            }
             if (sch == SCH_EXACT) {
                 // one pre-pass per stage writes every line's largest exponent
                 long long lines = 0, most = 0;

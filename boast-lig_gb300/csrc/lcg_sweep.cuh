@@ -31,6 +31,10 @@ struct Sweep {
     double a, a_x, a_y;
     double *dot_part;         // one partial per block (device), when has_dot
     long long le_off = 0;     // first entry of this sweep's lines in a batched line-exponent array
+    // tensor-core sweeps: the divisors of the tile index (output chunks per
+    // line block, line blocks per array, nL) with their multiplicative
+    // inverses, q = (n * m) >> s for every n < 2^31 (filled by tc_prepare)
+    unsigned int tdiv_d[3] = {1, 1, 1}, tdiv_m[3] = {0, 0, 0}, tdiv_s[3] = {0, 0, 0};
 };
 
 // Number of dot partials the FP64 sweep writes for S (grid size).

@@ -12,8 +12,8 @@ enum Scheme { SCH_EXACT = 0, SCH_BF16X3 = 1, SCH_TF32X3 = 2 };
 
 // Filter operand planes, one entry per tap of the flat filter (convolution:
 // the taps; wavelets: LE | LO | HE | HO), operator scalar folded in.
-//   SCH_EXACT: signed byte digits of the 64-bit fixed point as FP16 bit
-//     patterns, a*tap = 2^(ef-64) * sum_s dig[s] 256^(7-s);
+//   SCH_EXACT: balanced byte digits (in [-128, 127]) of the signed 62-bit
+//     fixed point as FP16 bit patterns, a*tap = 2^(ef-62) * sum_s dig[s] 256^(7-s);
 //   SCH_BF16X3: three bfloat16 terms (low 16 bits of dig[0..2]);
 //   SCH_TF32X3: two tf32 terms (FP32 bit patterns in dig[0..1]).
 struct TcFilter {
@@ -27,6 +27,9 @@ struct TcFilter {
 void tc_filter_digits(const double *taps, int ntaps, double a, TcFilter &F);
 void tc_filter_split(const double *taps, int ntaps, double a, int sch, TcFilter &F);
 bool sweep_tc_supported(const Sweep &S);
+// Fill S's tile-index divisors (Sweep::tdiv_*); false when the sweep has
+// 2^31 or more tiles or lines (the kernel's 32-bit tile arithmetic).
+bool tc_prepare(Sweep &S);
 // CTAs of the (non-batched) tensor-core sweep of S.  Its dot partials: 8
 // per CTA per array, array-major (sweep_tc_blocks(S) * 8 per array); the
 // slots of an array a CTA has no tile of are not written.

@@ -184,6 +184,28 @@ cudaError_t launch_line_exp3(const double *x, int n0, int n1, int n2, int narr, 
     return cudaGetLastError();
 }
 
+// Divisor d with its inverse for n < 2^31: s = 31 + ceil(log2 d),
+// m = ceil(2^s / d) < 2^32, floor(n / d) = (n m) >> s (the error term
+// n (m - 2^s / d) / 2^s stays below 1 / d).
+static void fast_div(unsigned int d, unsigned int &dd, unsigned int &m, unsigned int &s) {
+    unsigned int l = 0;
+    while ((1ull << l) < d) ++l;
+    dd = d;
+    s = 31 + l;
+    m = (unsigned int)(((1ull << s) + d - 1) / d);
+}
+
+bool tc_prepare(Sweep &S) {
+    const int qp = S.kind == KCONV ? 64 : 32;
+    const long long nlines = (long long)S.nL * S.nR;
+    const long long nch = (S.qhi - S.qlo + qp) / qp, nlb = (nlines + 127) / 128;
+    if (nlines < 1 || nlines >= (1LL << 31) || nch * nlb * S.narr >= (1LL << 31)) return false;
+    fast_div((unsigned int)nch, S.tdiv_d[0], S.tdiv_m[0], S.tdiv_s[0]);
+    fast_div((unsigned int)nlb, S.tdiv_d[1], S.tdiv_m[1], S.tdiv_s[1]);
+    fast_div((unsigned int)S.nL, S.tdiv_d[2], S.tdiv_m[2], S.tdiv_s[2]);
+    return true;
+}
+
 bool sweep_tc_supported(const Sweep &S) {
     if (S.kind == KCONV) return S.ntaps == 16 || S.ntaps == 17 || S.ntaps == 29;
     return (S.kind == KDEC || S.kind == KREC) && (S.ntaps == 8 || S.ntaps == 16);
@@ -195,10 +217,14 @@ long long sweep_tc_blocks(const Sweep &S) {
     return tiles < sms ? tiles : sms;
 }
 
-// Filter bytes with the operator scalar folded in exactly: a*f is formed as
-// the 106-bit product of the two mantissas, then rounded once to the 64-bit
-// fixed point |a f| 2^(64 - ef) (ef: power of two above the largest |a f| of
-// the whole flat filter, so every channel pair shares one scale).
+// Filter digits with the operator scalar folded in exactly: a*f is formed as
+// the 106-bit product of the two mantissas, then rounded once to the signed
+// fixed point F = a f 2^(62 - ef), |F| <= 2^62 (ef: power of two above the
+// largest |a f| of the whole flat filter, so every channel pair shares one
+// scale; raised further while the sum of |a f| reaches 8 * 2^ef, which keeps
+// the kernel's recombined 64-bit result below 2^61).  F is cut into 8
+// balanced byte digits e_0 (top) .. e_7 in [-128, 127]:
+// F = sum_t e_t 256^(7-t), the bytes of F + 0x8080808080808080 minus 128.
 void tc_filter_digits(const double *taps, int ntaps, double a, TcFilter &F) {
     memset(&F, 0, sizeof(F));
     int ea = 0;
@@ -207,12 +233,14 @@ void tc_filter_digits(const double *taps, int ntaps, double a, TcFilter &F) {
     unsigned __int128 prod[TcFilter::kMaxTaps];
     int ep[TcFilter::kMaxTaps];
     int ef = -100000;
+    double sum = 0.0;
     for (int i = 0; i < ntaps; ++i) {
         int e = 0;
         const double ff = frexp(fabs(taps[i]), &e);
         const unsigned long long mf = (unsigned long long)ldexp(ff, 53);
         prod[i] = (unsigned __int128)ma * mf;
         ep[i] = (ea - 53) + (e - 53);                               // |a f| = prod 2^ep
+        sum += fabs(a * taps[i]);
         if (prod[i]) {
             int bl = 0;
             for (unsigned __int128 t = prod[i]; t; t >>= 1) ++bl;
@@ -220,18 +248,21 @@ void tc_filter_digits(const double *taps, int ntaps, double a, TcFilter &F) {
         }
     }
     if (ef == -100000) ef = 0;
+    while (sum >= ldexp(8.0, ef)) ++ef;
     F.ef = ef;
     for (int i = 0; i < ntaps; ++i) {
-        const int sh = ep[i] + 64 - ef;                             // |F| = prod 2^sh < 2^64
+        const int sh = ep[i] + 62 - ef;                             // |F| = prod 2^sh <= 2^62
         const unsigned __int128 v = prod[i];
-        unsigned long long X;
-        if (sh >= 0) X = (unsigned long long)(v << sh);
-        else if (-sh >= 127) X = 0;
-        else X = (unsigned long long)((v + ((unsigned __int128)1 << (-sh - 1))) >> (-sh));
+        unsigned long long M;
+        if (sh >= 0) M = (unsigned long long)(v << sh);
+        else if (-sh >= 127) M = 0;
+        else M = (unsigned long long)((v + ((unsigned __int128)1 << (-sh - 1))) >> (-sh));
         const bool neg = (a < 0) != (taps[i] < 0);
-        for (int s = 0; s < TcFilter::kSlices; ++s) {
-            const int byte = (int)((X >> (8 * (7 - s))) & 0xFF);
-            F.dig[s][i] = __half_as_ushort(__int2half_rn(neg ? -byte : byte));
+        const unsigned long long X = neg ? 0ull - M : M;           // two's complement
+        const unsigned long long U = X + 0x8080808080808080ull;
+        for (int t = 0; t < TcFilter::kSlices; ++t) {
+            const int digit = (int)((U >> (8 * (7 - t))) & 0xFF) - 128;
+            F.dig[t][i] = __half_as_ushort(__int2half_rn(digit));
         }
     }
 }

@@ -10,22 +10,25 @@
 //
 // Scheme SCH_EXACT (FP64-accurate, exact integer arithmetic on FP16 operands)
 //   * each line segment of a tile is scaled by the power of two above its
-//     largest magnitude to 64-bit integers |X| < 2^64; the 8 bytes of |X| are
-//     the digits d_0 (top byte) .. d_7, exact in FP16 with the sign of x;
+//     largest magnitude to signed 62-bit integers X = x 2^(62-E) (|X| <=
+//     2^62, truncated toward zero); X is cut into 8 balanced byte digits
+//     d_0 (top) .. d_7 in [-128, 127], X = sum_s d_s 256^(7-s): the bytes
+//     of X + 0x8080808080808080 minus 128, exact in FP16;
 //   * the filter, with the operator scalar a folded in exactly (128-bit
-//     product of the two mantissas), is cut the same way into bytes e_0..e_7;
-//   * byte-pair products are below 2^16 and every partial sum over <= 32
-//     products x 8 pairs stays below 2^24, so FP32 accumulation in TMEM is
-//     exact;
-//   * pairs of order k = s + t <= 6 (16 products per output: MagicFilter,
-//     sym8 wavelets; 28 pairs) or <= 7 (29 or 32 products: kinetic, derivative,
-//     MagicFilter-combined wavelets, whose large alternating taps cancel; 36
-//     pairs) are accumulated, one TMEM accumulator per order; the epilogue
-//     recombines Y = sum_{k<=5} Acc_k 2^(8(5-k)) + Acc_6 2^-8 + Acc_7 2^-16 in
-//     int64, converts once and rescales the exponent.
-//   Dropped orders weigh <= 2^-64 of the line scale: at least as accurate as
-//   an FP64 FMA chain.  Lines never share a scale; a line segment holding an
-//   Inf or NaN gives NaN on that tile row.
+//     product of the two mantissas), is cut the same way into e_0..e_7;
+//   * byte-pair products are at most 2^14 in magnitude and every partial
+//     sum over <= 32 products x 8 pairs stays within 2^22, so FP32
+//     accumulation in TMEM is exact and every accumulator converts to an
+//     integer with one FP32 add;
+//   * the 36 pairs of order k = s + t <= 7 are accumulated, one TMEM
+//     accumulator per order; the epilogue recombines
+//     Y = sum_k Acc_k 2^(46-8k) in int64 (the orders 6-7 rounded to an
+//     integer first), converts once and rescales the exponent.
+//   Dropped orders (k >= 8) weigh below 2^-70 of the product of the line and
+//   filter scales; the data truncation (2^-62 of the line scale) and the
+//   final roundings stay below the rounding of an FP64 FMA chain.
+//   Lines never share a scale; a line segment holding an Inf or NaN gives
+//   NaN on that tile row.
 //
 // Split-precision schemes (FP32-class accuracy, reported per operator)
 //   * every element is rounded to FP32 (magnitudes outside the normal float
@@ -82,7 +85,7 @@ template <int KIND, int NT, int SCH> struct Geom {
     static constexpr int ESZ = SCH == SCH_TF32X3 ? 4 : 2;         // operand element bytes
     static constexpr int CE = 16 / ESZ;                          // elements per core-matrix row
     static constexpr int MK = 32 / ESZ;                          // K of one MMA
-    static constexpr int ND = SCH == SCH_EXACT ? (PROD > 16 ? 8 : 7) : SCH == SCH_BF16X3 ? 3 : 2;
+    static constexpr int ND = SCH == SCH_EXACT ? 8 : SCH == SCH_BF16X3 ? 3 : 2;
     static constexpr int ORD = ND;                               // order accumulators per block
     static constexpr int BN = 16 * ORD;                          // rows of the stacked filter
     static constexpr int LBO_B = BN * 16;                        // its K-direction chunk stride
@@ -212,10 +215,11 @@ __device__ __forceinline__ double ll_scaled(long long Y, int se) {
 }
 
 // The same conversion without branches, for the common case: `bad` records
-// a zero-or-subnormal-or-infinite result exponent (the caller then redoes
-// the conversion with ll_scaled).  |Y| is normalised so its leading one is
-// bit 63; bits 10..0 below the 53-bit mantissa give round-to-nearest-even,
-// and a carry out of the mantissa moves into the exponent field.
+// a subnormal-or-infinite result exponent (the caller then redoes the
+// conversion with ll_scaled).  |Y| is normalised so its leading one is bit
+// 63; the 11 bits below the 53-bit mantissa and its last bit give
+// round-to-nearest-even (an increment exactly when low + lsb + 0x3FF carries
+// into bit 11), and a carry out of the mantissa moves into the exponent field.
 __device__ __forceinline__ double ll_scaled_fast(long long Y, int se, bool &bad) {
     const unsigned long long u = (unsigned long long)Y;
     const unsigned long long s = (unsigned long long)(Y >> 63);
@@ -223,48 +227,44 @@ __device__ __forceinline__ double ll_scaled_fast(long long Y, int se, bool &bad)
     const int lz = __clzll((long long)a);                        // 64 when Y == 0
     const unsigned long long nrm = a << (lz & 63);
     const unsigned long long mant = nrm >> 11;                   // leading one at bit 52
-    const unsigned long long inc =
-        ((nrm >> 10) & 1ull) & ((unsigned long long)((nrm & 0x3FFull) != 0) | (mant & 1ull));
+    const uint32_t nl = (uint32_t)nrm;
+    const uint32_t inc = ((nl & 0x7FFu) + ((nl >> 11) & 1u) + 0x3FFu) >> 11;
     const int be = 1086 - lz + se;                               // exponent field
-    bad |= !(be >= 1 && be <= 2046);
-    const unsigned long long bits =
-        (u & 0x8000000000000000ull) | (((unsigned long long)(be - 1) << 52) + mant + inc);
+    bad |= (unsigned)(be - 1) > 2045u;
+    const unsigned long long bits = (u & 0x8000000000000000ull) +
+                                    (((unsigned long long)(be - 1) << 52) + mant + inc);
     return Y == 0 ? 0.0 : __longlong_as_double((long long)bits);
 }
 
-// Bits of an FP32 accumulator plus 1.5 * 2^23 (the integer sits in the low
-// mantissa bits, biased by 0x4B400000, when |v| < 2^22; `big` records a
-// larger magnitude).
-__device__ __forceinline__ uint32_t acc_bits(uint32_t u, bool &big) {
-    const float f = __uint_as_float(u);
-    big |= !(fabsf(f) < 4194304.0f);
-    return __float_as_uint(f + 12582912.0f);
+// Bits of an FP32 accumulator plus 1.5 * 2^23: the integer value v of the
+// accumulator (|v| <= 2^22 by the digit bounds) sits in the low mantissa bits,
+// biased: bits = 0x4B400000 + v.
+__device__ __forceinline__ uint32_t acc_bits(uint32_t u) {
+    return __float_as_uint(__uint_as_float(u) + 12582912.0f);
 }
 
-// sum_{k<6} v_k 2^(8(5-k)) from the biased bits b_k = v_k + 0x4B400000 of
-// acc_bits: Horner modulo 2^64 on the biased bits (three 32x32+64
-// multiply-adds for the low terms, one 32-bit add into the high word for
-// the two top terms), then the bias of all six terms removed at once.  The
-// wrap-around is exact because the true sum fits in 64 bits.
-__device__ __forceinline__ long long horner6(const uint32_t (&b)[6]) {
-    constexpr unsigned long long kBias =
-        0x4B400000ull * ((1ull << 40) + (1ull << 32) + (1ull << 24) + (1ull << 16) + (1ull << 8) + 1ull);
-    unsigned long long v = b[5];
-    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(v) : "r"(b[4]), "r"(256u), "l"(v));
-    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(v) : "r"(b[3]), "r"(65536u), "l"(v));
-    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(v) : "r"(b[2]), "r"(16777216u), "l"(v));
-    v += (unsigned long long)(b[1] + (b[0] << 8)) << 32;
-    return (long long)(v - kBias);
-}
-
-// Integer value of an FP32 accumulator (an exact integer): one FP32 add of
-// 1.5 * 2^23 leaves it in the low mantissa bits when |v| < 2^22 (ulp 1 in
-// [2^23, 2^24)); `big` records a larger magnitude (the caller then converts
-// with the conversion instruction, which runs on the narrow FP64 pipe here).
-__device__ __forceinline__ int acc_int(uint32_t u, bool &big) {
-    const float f = __uint_as_float(u);
-    big |= !(fabsf(f) < 4194304.0f);
-    return __float_as_int(f + 12582912.0f) - 0x4B400000;
+// Y = sum_k Acc_k 2^(46 - 8k) over the 8 order accumulators of one output,
+// from their biased bits b_k = Acc_k + 0x4B400000 (acc_bits): orders 0-5 by
+// Horner modulo 2^64 (three 32x32+64 multiply-adds for the low terms, a
+// 32-bit add into the high word for the two top terms), orders 6-7 as the
+// nearest integer of Acc_6 / 4 + Acc_7 / 1024 (one 32-bit multiply-add and
+// an arithmetic shift, exact because that sum fits in 31 bits), then the
+// bias of every term removed by one 64-bit constant.  The wrap-around is
+// exact because the true sum fits in 62 bits.
+template <int ORD>
+__device__ __forceinline__ long long horner_bal(const uint32_t (&b)[ORD]) {
+    static_assert(ORD == 8, "eight order accumulators");
+    constexpr unsigned long long kW = (1ull << 46) + (1ull << 38) + (1ull << 30) + (1ull << 22) +
+                                      (1ull << 14) + (1ull << 6);
+    constexpr unsigned long long kBias = 0x4B400000ull * kW;
+    unsigned long long v = (unsigned long long)b[5] << 6;
+    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(v) : "r"(b[4]), "r"(16384u), "l"(v));
+    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(v) : "r"(b[3]), "r"(4194304u), "l"(v));
+    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(v) : "r"(b[2]), "r"(1073741824u), "l"(v));
+    v += (unsigned long long)(b[1] * 64u + b[0] * 16384u) << 32;
+    // (Acc_6 * 256 + Acc_7 + 512) >> 10, the biases folded into one constant
+    const int lo = (int)(b[6] * 256u + b[7] + (512u - 257u * 0x4B400000u)) >> 10;
+    return (long long)(v - kBias) + (long long)lo;
 }
 
 // FP32 bits -> FP64 value, integer only (normal, zero, subnormal flushed, inf/nan).
@@ -276,45 +276,38 @@ __device__ __forceinline__ double f32_to_f64(uint32_t f) {
     return __longlong_as_double((long long)b);
 }
 
-// Fixed-point magnitude |X| = round(|x| 2^(64-E)) of the FP64 bit pattern
-// (|x| < 2^E), split in 32-bit words, and the sign bit.  Integer only:
-// left shifts (values within 2^11 of the row maximum) are two funnel shifts.
-__device__ __forceinline__ void fixed64(long long bits, int E, uint32_t &xl, uint32_t &xh,
-                                        uint32_t &sgn) {
+// Balanced fixed point of one FP64 bit pattern against its line's largest
+// exponent field mx (>= 1): U = X + 0x8080808080808080 with X = x 2^(62-E),
+// E = mx - 1022, truncated toward zero; integer only, no branch: the 53-bit
+// mantissa shifted up by 10 (below 2^63), then right by 10 - sh in [0, 63]
+// where X = mant 2^sh (sh <= 9 since the element's exponent is at most mx;
+// a shift of 63 leaves 0), sign applied in two's complement, bias added.
+__device__ __forceinline__ void fixed_bal(long long bits, int mx, uint32_t &ul, uint32_t &uh) {
     const uint32_t lo = (uint32_t)bits, hi = (uint32_t)((unsigned long long)bits >> 32);
-    int ex = (int)((hi >> 20) & 0x7FF);
-    uint32_t mh = hi & 0xFFFFFu;
-    if (ex) mh |= 0x100000u;
-    else ex = 1;
-    sgn = hi >> 31;
-    const int r = E - (ex - 1022);                       // |X| = mant 2^(11 - r)
-    if (r <= 11) {
-        const uint32_t c = (uint32_t)(11 - r);           // 0..11
-        xh = __funnelshift_l(lo, mh, c);
-        xl = lo << c;
-    } else {
-        const int c = r - 11;                            // right shift with rounding
-        if (c >= 64) { xl = xh = 0; return; }
-        unsigned long long m = ((unsigned long long)mh << 32) | lo;
-        m = (m + (1ull << (c - 1))) >> c;
-        xl = (uint32_t)m;
-        xh = (uint32_t)(m >> 32);
-    }
+    const int ex = (int)((hi >> 20) & 0x7FF);
+    const uint32_t mh = (hi & 0xFFFFFu) | (ex ? 0x100000u : 0u);
+    const int c = min(max(mx - max(ex, 1) + 1, 0), 63);         // 10 - sh
+    const unsigned long long m10 = (((unsigned long long)mh << 32) | lo) << 10;
+    const unsigned long long M = m10 >> c;
+    const unsigned long long sg = (unsigned long long)(bits >> 63);   // 0 or all ones
+    const unsigned long long U = (M ^ sg) + (sg & 1ull) + 0x8080808080808080ull;
+    ul = (uint32_t)U;
+    uh = (uint32_t)(U >> 32);
 }
 
-// half2 of byte b (0 = lowest) of two fixed-point magnitudes, with their
-// signs: PRMT gathers the bytes, 0x6400 makes them 1024 + d in FP16, and one
-// HFMA2 applies +-1 and removes the 1024 (exact).
-__device__ __forceinline__ uint32_t digit_pair(int b, uint32_t al, uint32_t ah, uint32_t bl,
-                                               uint32_t bh, uint32_t smul, uint32_t sadd) {
-    const uint32_t wa = b >= 4 ? ah : al;
-    const uint32_t wb = b >= 4 ? bh : bl;
-    const uint32_t sel = (uint32_t)(b & 3) | ((uint32_t)(4 + (b & 3)) << 8);
+// FP16 pair of balanced digit b (0 = lowest byte) of two biased fixed points
+// (ul/uh of elements a and b): PRMT gathers the two bytes, 0x6400 makes them
+// 1024 + byte in FP16, one HADD2 subtracts 1024 + 128 (exact).
+__device__ __forceinline__ uint32_t digit_pair_bal(int byte, uint32_t al, uint32_t ah, uint32_t bl,
+                                                   uint32_t bh) {
+    const uint32_t wa = byte >= 4 ? ah : al;
+    const uint32_t wb = byte >= 4 ? bh : bl;
+    const uint32_t sel = (uint32_t)(byte & 3) | ((uint32_t)(4 + (byte & 3)) << 8);   // bytes 0, 2
     uint32_t t;
     asm("prmt.b32 %0, %1, %2, %3;" : "=r"(t) : "r"(wa), "r"(wb), "r"(sel));
     t = (t & 0x00FF00FFu) | 0x64006400u;
-    __half2 h = *reinterpret_cast<__half2 *>(&t);
-    h = __hfma2(h, *reinterpret_cast<const __half2 *>(&smul), *reinterpret_cast<const __half2 *>(&sadd));
+    const uint32_t off = 0xE480E480u;                            // (-1152, -1152) in FP16
+    __half2 h = __hadd2(*reinterpret_cast<__half2 *>(&t), *reinterpret_cast<const __half2 *>(&off));
     return *reinterpret_cast<uint32_t *>(&h);
 }
 
@@ -389,26 +382,48 @@ __device__ __forceinline__ int filter_index(int c, int c2) {
     return c == 0 ? (c2 == 0 ? 1 : 3) : (c2 == 0 ? 0 : 2);          // KREC
 }
 
-// Where tile `tile` of a launch lives: its sweep and its index within the
-// sweep.  A batched launch (BATCH) covers a list of sweeps of the same kind
-// and filter, one per grid of a batch of uneven grids, whose tiles are
-// numbered consecutively (prefix[i] = first tile of sweep i).
+// floor(n / d) for n < 2^31 with d's multiplicative inverse (tc_prepare).
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, uint32_t m, uint32_t s) {
+    return (uint32_t)(((unsigned long long)n * m) >> s);
+}
+
+// Where tile `tile` of a launch lives: its sweep, its output chunk `ch`
+// along the lines, its block of kM lines `lb` and its array.  Tiles are
+// numbered chunk fastest, then line block, then array.  A batched launch
+// (BATCH) covers a list of sweeps of the same kind and filter, one per grid
+// of a batch of uneven grids, whose tiles are numbered consecutively
+// (prefix[i] = first tile of sweep i).
 struct TileLoc {
     const Sweep *S;
-    long long t;
+    int ch;
+    uint32_t lb;
+    int arr;
 };
 
 template <bool BATCH>
 __device__ __forceinline__ TileLoc locate(const Sweep &S0, const Sweep *descs,
                                           const long long *prefix, int nsweeps, long long tile) {
-    if (!BATCH) return {&S0, tile};
-    int lo = 0, hi = nsweeps - 1;                        // last i with prefix[i] <= tile
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (prefix[mid] <= tile) lo = mid;
-        else hi = mid - 1;
+    const Sweep *S = &S0;
+    uint32_t t = (uint32_t)tile;
+    if (BATCH) {
+        int lo = 0, hi = nsweeps - 1;                    // last i with prefix[i] <= tile
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (prefix[mid] <= tile) lo = mid;
+            else hi = mid - 1;
+        }
+        S = descs + lo;
+        t = (uint32_t)(tile - prefix[lo]);
     }
-    return {descs + lo, tile - prefix[lo]};
+    const uint32_t q = fdiv(t, S->tdiv_m[0], S->tdiv_s[0]);          // t / chunks
+    const uint32_t arr = fdiv(q, S->tdiv_m[1], S->tdiv_s[1]);        // / line blocks
+    return {S, (int)(t - q * S->tdiv_d[0]), q - arr * S->tdiv_d[1], (int)arr};
+}
+
+// Line g of a sweep as (l, r): g = l + nL r.
+__device__ __forceinline__ void line_lr(const Sweep &S, uint32_t g, uint32_t &l, uint32_t &r) {
+    r = fdiv(g, S.tdiv_m[2], S.tdiv_s[2]);
+    l = g - r * S.tdiv_d[2];
 }
 
 template <int KIND, int NT, int SCH, bool BATCH>
@@ -502,16 +517,10 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
         for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
             const TileLoc loc = locate<BATCH>(S0, descs, prefix, nsweeps, tile);
             const Sweep &S = *loc.S;
-            const long long nlines = (long long)S.nL * S.nR;
-            const long long nlb = (nlines + kM - 1) / kM;
-            const int nch = (S.qhi - S.qlo + G::QP) / G::QP;
-            const int ch = (int)(loc.t % nch);
-            const long long lb = (loc.t / nch) % nlb;
-            const int arr = (int)(loc.t / (nch * nlb));
+            const uint32_t nlines = (uint32_t)S.nL * (uint32_t)S.nR;
             const int plast = S.qhi + S.lowfil + NT - 1;                // last input position used
-            const long long *xbits = reinterpret_cast<const long long *>(S.x);
             const long long in_ext = S.in_ext;
-            const int p0 = S.qlo + ch * G::QP + S.lowfil;               // first input position
+            const int p0 = S.qlo + loc.ch * G::QP + S.lowfil;           // first input position
             const int pstart = S.bc == BC_PERIODIC ? imod(p0, S.n) : 0;
             const bool onewrap = S.n >= G::KT;
             // element kk of the tile -> offset (in elements) in the line, -1 for a zero
@@ -531,59 +540,61 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                 }
                 return KIND == KCONV ? ps : KIND == KDEC ? (long long)c + 2LL * ps : ps + in_ext * c;
             };
-            const long long g = lb * kM + row;
+            const uint32_t g = loc.lb * kM + row;
             const bool valid = g < nlines;
-            const long long l = valid ? g % S.nL : 0, r = valid ? g / S.nL : 0;
-            const long long *base = xbits + (long long)arr * S.x_arr + l + (long long)S.nL * (in_ext * NCH) * r;
+            uint32_t l = 0, r = 0;
+            if (valid) line_lr(S, g, l, r);
+            const long long *base = reinterpret_cast<const long long *>(S.x) + (long long)loc.arr * S.x_arr +
+                                    l + (long long)S.nL * (in_ext * NCH) * r;
             const long long stride = S.nL;
             const int klim = min(kneed, NCH * (plast - p0 + 1));
-            // contiguous fast path: the row's valid elements [0, klim) are one
-            // unbroken 16-byte aligned run (one check per row), or else the
-            // group's own valid elements are (a segment that wraps or starts
-            // outside a free line)
-            const bool lin = KIND != KREC && stride == 1 && valid && klim > 0;
-            const long long of0 = lin ? off_of(0) : -1;
-            const bool run_all = lin && of0 >= 0 && off_of(klim - 1) == of0 + klim - 1 &&
-                                 ((((uintptr_t)(base + of0)) & 15) == 0);
-            // the 8 elements of group gi
+            // the 8 elements of group gi.  The group's first cnt elements are
+            // used (the same for every row of the tile); when their line
+            // offsets are one consecutive run (inside the line, no wrap) they
+            // are loaded from one pointer -- 16-byte vectors along contiguous
+            // lines -- else element by element
             auto load8 = [&](int gi, long long (&bits)[8]) {
                 const int i0 = gi * 8;
                 const int cnt = max(0, min(8, klim - i0));
-                long long oa = -1, ob = -2;
-                if (run_all) {
-                    oa = of0 + i0;
-                    ob = oa + cnt - 1;
-                } else if (lin && cnt > 0) {
-                    oa = off_of(i0);
-                    ob = off_of(i0 + cnt - 1);
+                long long oa = -1;
+                if (KIND != KREC && cnt > 0) {
+                    const long long a0 = off_of(i0);
+                    if (a0 >= 0 && off_of(i0 + cnt - 1) == a0 + cnt - 1) oa = a0;
                 }
-                if (oa >= 0 && ob == oa + cnt - 1 && ((((uintptr_t)(base + oa)) & 15) == 0)) {
-                    const double2 *v = reinterpret_cast<const double2 *>(base + oa);
+                if (oa >= 0) {
+                    const long long *q = base + oa * stride;
+                    if (stride == 1 && ((((uintptr_t)q) & 15) == 0)) {
+                        const double2 *v = reinterpret_cast<const double2 *>(q);
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const int i = 2 * e;
-                        if (i + 1 < cnt) {
-                            const double2 t = v[e];
-                            bits[2 * e] = __double_as_longlong(t.x);
-                            bits[2 * e + 1] = __double_as_longlong(t.y);
-                        } else {
-                            bits[2 * e] = i < cnt ? base[oa + i] : 0ll;
-                            bits[2 * e + 1] = 0ll;
+                        for (int e = 0; e < 4; ++e) {
+                            if (valid && 2 * e + 1 < cnt) {
+                                const double2 t = v[e];
+                                bits[2 * e] = __double_as_longlong(t.x);
+                                bits[2 * e + 1] = __double_as_longlong(t.y);
+                            } else {
+                                bits[2 * e] = (valid && 2 * e < cnt) ? q[2 * e] : 0ll;
+                                bits[2 * e + 1] = 0ll;
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) {
+                            bits[e] = (valid && e < cnt) ? *q : 0ll;
+                            q += stride;
                         }
                     }
                 } else {
 #pragma unroll
                     for (int e = 0; e < 8; ++e) {
-                        const long long o = valid ? off_of(i0 + e) : -1;
+                        const long long o = (valid && e < cnt) ? off_of(i0 + e) : -1;
                         bits[e] = o >= 0 ? base[o * stride] : 0ll;
                     }
                 }
             };
-            int mx = 0, E = 0;
+            int mx = 0;
             if (SCH == SCH_EXACT && lineE) {
                 // largest exponent field of the line (line_exp_kernel)
-                mx = valid ? lineE[S.le_off + (long long)arr * nlines + g] : 0;
-                E = (mx ? mx : 1) - 1022;
+                mx = valid ? lineE[S.le_off + (long long)loc.arr * nlines + g] : 0;
             } else if (SCH == SCH_EXACT) {
 #pragma unroll
                 for (int c0 = 0; c0 < NGH; c0 += 2) {            // 16 loads in flight
@@ -600,8 +611,8 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                                          (int)(((unsigned long long)b1[e] >> 52) & 0x7FF)));
                 }
                 mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
-                E = (mx ? mx : 1) - 1022;
             }
+            const int mxe = max(mx, 1);
             // software pipeline: the next group's loads are in flight while the
             // current group is cut into digits
             long long bits[8], nxt[8];
@@ -619,22 +630,15 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                 // 8 elements = 8 / CE core-matrix chunks of 2048 bytes (128 rows)
                 const int off = group_of(c) * (8 / G::CE) * 2048 + (row >> 3) * 128 + (row & 7) * 16;
                 if (SCH == SCH_EXACT) {
-                    uint32_t xl[8], xh[8], sg[8];
+                    uint32_t ul[8], uh[8];
 #pragma unroll
-                    for (int e = 0; e < 8; ++e) fixed64(bits[e], E, xl[e], xh[e], sg[e]);
-                    uint32_t smul[4], sadd[4];
-#pragma unroll
-                    for (int w = 0; w < 4; ++w) {
-                        smul[w] = (0x3C00u | (sg[2 * w] << 15)) | ((0x3C00u | (sg[2 * w + 1] << 15)) << 16);
-                        sadd[w] = (0xE400u ^ (sg[2 * w] << 15)) | ((0xE400u ^ (sg[2 * w + 1] << 15)) << 16);
-                    }
+                    for (int e = 0; e < 8; ++e) fixed_bal(bits[e], mxe, ul[e], uh[e]);
 #pragma unroll
                     for (int sd = 0; sd < G::ND; ++sd) {
                         uint32_t wds[4];
 #pragma unroll
                         for (int w = 0; w < 4; ++w)
-                            wds[w] = digit_pair(7 - sd, xl[2 * w], xh[2 * w], xl[2 * w + 1], xh[2 * w + 1],
-                                                smul[w], sadd[w]);
+                            wds[w] = digit_pair_bal(7 - sd, ul[2 * w], uh[2 * w], ul[2 * w + 1], uh[2 * w + 1]);
                         *(uint4 *)(A + sd * G::A_PLANE + off) = make_uint4(wds[0], wds[1], wds[2], wds[3]);
                     }
                 } else if (SCH == SCH_BF16X3) {
@@ -661,7 +665,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
 #pragma unroll
                 for (int e = 0; e < 8; ++e) bits[e] = nxt[e];
                 if (c == 1 || c == 3 || c == NGH - 1) {          // last group of a pair
-                    if (c == 1 && half == 0) rowE3[(it % 3) * kM + row] = mx == 0x7FF ? 0x7FFFFFFF : E;
+                    if (c == 1 && half == 0) rowE3[(it % 3) * kM + row] = mx == 0x7FF ? 0x7FFFFFFF : mxe - 1022;
                     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
                     bar_arrive(pfull[c == 1 ? 0 : c == 3 ? 1 : 2]);
                 }
@@ -707,21 +711,19 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             const int Er = rowE3[(it % 3) * kM + row];
             const TileLoc loc = locate<BATCH>(S0, descs, prefix, nsweeps, tile);
             const Sweep &S = *loc.S;
-            const long long nlines = (long long)S.nL * S.nR;
-            const long long nlb = (nlines + kM - 1) / kM;
-            const int nch = (S.qhi - S.qlo + G::QP) / G::QP;
-            const int ch = (int)(loc.t % nch);
-            const long long lb = (loc.t / nch) % nlb;
-            const int arr = (int)(loc.t / (nch * nlb));
+            const int arr = loc.arr;
             if (!BATCH && S0.has_dot && arr != dot_arr) {
                 if (dot_arr >= 0) flush_dot();
                 dot_arr = arr;
             }
-            const int qc0 = S.qlo + ch * G::QP;
+            const int qc0 = S.qlo + loc.ch * G::QP;
             const long long out_pext = (long long)S.out_ext * NCH;
-            const long long g = lb * kM + row;
+            const uint32_t nlines = (uint32_t)S.nL * (uint32_t)S.nR;
+            const uint32_t g = loc.lb * kM + row;
             const bool valid = g < nlines;
-            const long long l = valid ? g % S.nL : 0, rr = valid ? g / S.nL : 0;
+            uint32_t l32 = 0, r32 = 0;
+            if (valid) line_lr(S, g, l32, r32);
+            const long long l = l32, rr = r32;
             double *__restrict__ y = S.y + (long long)arr * S.y_arr;
             const double *__restrict__ xa = S.x + (long long)arr * S.x_arr;
             const double *__restrict__ x2 = S.x2 ? S.x2 + (long long)arr * S.x_arr : nullptr;
@@ -739,7 +741,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             const long long x2s = grow ? ys : S.nL;
             const int x2lo = grow ? S.out_lo : S.in_lo;
             const double *const xrow = xa + l + (long long)S.nL * S.in_ext * rr;
-            const int se = Er + F.ef - 56;
+            const int se = Er + F.ef - 58;
             const bool nanrow = SCH == SCH_EXACT && Er == 0x7FFFFFFF;
 #pragma unroll 1
             for (int step = 0; step < 4; ++step) {             // 2 blocks x 2 x 8 outputs
@@ -758,9 +760,12 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                 double *const ystep = yrow + yps * (q0 - S.out_lo);
                 double add[8];
                 if (KIND == KCONV && x2) {
-                    const double *const x2step = x2row + x2s * (q0 - x2lo);
+                    const double *xp = x2row + x2s * (q0 - x2lo);
 #pragma unroll
-                    for (int n = 0; n < 8; ++n) add[n] = n < nv ? x2step[x2s * n] : 0.0;
+                    for (int n = 0; n < 8; ++n) {
+                        add[n] = n < nv ? *xp : 0.0;
+                        xp += x2s;
+                    }
                 }
                 {
                     // 4 outputs at a time: their values first (independent,
@@ -769,33 +774,15 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                     for (int g0 = 0; g0 < 8; g0 += 4) {
                         if (g0 >= nv) continue;
                         double outv[4];
-                        if (SCH == SCH_EXACT) {
-                            bool big = false, bad = false;
+                        if constexpr (SCH == SCH_EXACT) {
+                            bool bad = false;
                             long long Y[4];
 #pragma unroll
                             for (int i = 0; i < 4; ++i) {
-                                const int n = g0 + i;
-                                uint32_t bb[6];
+                                uint32_t bb[G::ORD];
 #pragma unroll
-                                for (int k = 0; k < 6; ++k) bb[k] = acc_bits(acc[k][n], big);
-                                const long long v = horner6(bb);
-                                int lo = acc_int(acc[6][n], big);
-                                if (G::ORD > 7) lo += (acc_int(acc[G::ORD - 1][n], big) + 128) >> 8;
-                                Y[i] = v + (((long long)lo + 128) >> 8);
-                            }
-                            if (big) {                    // an accumulator >= 2^22: exact path
-#pragma unroll
-                                for (int i = 0; i < 4; ++i) {
-                                    const int n = g0 + i;
-                                    long long v = __float2int_rn(__uint_as_float(acc[0][n]));
-#pragma unroll
-                                    for (int k = 1; k < 6; ++k)
-                                        v = v * 256 + __float2int_rn(__uint_as_float(acc[k][n]));
-                                    int lo = __float2int_rn(__uint_as_float(acc[6][n]));
-                                    if (G::ORD > 7)
-                                        lo += (__float2int_rn(__uint_as_float(acc[G::ORD - 1][n])) + 128) >> 8;
-                                    Y[i] = v + (((long long)lo + 128) >> 8);
-                                }
+                                for (int k = 0; k < G::ORD; ++k) bb[k] = acc_bits(acc[k][g0 + i]);
+                                Y[i] = horner_bal<G::ORD>(bb);
                             }
 #pragma unroll
                             for (int i = 0; i < 4; ++i) outv[i] = ll_scaled_fast(Y[i], se, bad);
@@ -816,13 +803,14 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                                 outv[i] = f32_to_f64(__float_as_uint(f));
                             }
                         }
+                        double *yq = ystep + yps * (g0 / NCH);   // position of output g0
 #pragma unroll
                         for (int i = 0; i < 4; ++i) {
                             const int n = g0 + i;
                             const int q = q0 + n / NCH, c = n % NCH;
                             if (n >= nv) break;
                             double out = outv[i];
-                            double *const yp = ystep + yps * (n / NCH) + ycs * c;
+                            double *const yp = c ? yq + ycs * c : yq;
                             if (KIND == KCONV) {
                                 const bool want_dot = !BATCH && S.has_dot;   // batched sweeps have no dot
                                 if ((want_dot || S.has_ax) && (!grow || (q >= 0 && q < S.n))) {
@@ -836,6 +824,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                             if (S.ay_mode == 2) out += *yp;
                             else if (S.ay_mode == 1) out = fma(S.a_y, *yp, out);
                             *yp = out;
+                            if (c == NCH - 1) yq += yps;
                         }
                     }
                 }
@@ -873,9 +862,11 @@ cudaError_t set_smem_attr() {
 }
 
 template <int KIND, int NT, int SCH>
-cudaError_t launch(const Sweep &S, const TcFilter &F, int *status, const int *lineE,
+cudaError_t launch(const Sweep &S_in, const TcFilter &F, int *status, const int *lineE,
                    cudaStream_t st) {
     using G = Geom<KIND, NT, SCH>;
+    Sweep S = S_in;
+    if (!tc_prepare(S)) return cudaErrorInvalidValue;
     cudaError_t e = set_smem_attr<KIND, NT, SCH, false>();
     if (e != cudaSuccess) return e;
     const long long tiles = tile_count_for(S, G::QP);
