@@ -35,6 +35,10 @@ struct Sweep {
     // line block, line blocks per array, nL) with their multiplicative
     // inverses, q = (n * m) >> s for every n < 2^31 (filled by tc_prepare)
     unsigned int tdiv_d[3] = {1, 1, 1}, tdiv_m[3] = {0, 0, 0}, tdiv_s[3] = {0, 0, 0};
+    // tensor-core convolution sweeps: the tile's input window starts woff
+    // elements before the first input position, so that along contiguous
+    // lines its 8-element groups start on 32-byte boundaries (0 otherwise)
+    int woff = 0;
 };
 
 // Number of dot partials the FP64 sweep writes for S (grid size).

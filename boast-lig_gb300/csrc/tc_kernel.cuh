@@ -184,6 +184,12 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
                  : "memory");
 }
 
+// 32 bytes from global memory (a 32-byte aligned address) in one load.
+__device__ __forceinline__ void ld256(const long long *p, long long &a, long long &b, long long &c,
+                                      long long &d) {
+    asm("ld.global.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p));
+}
+
 __device__ __forceinline__ int imod(int a, int n) {
     int r = a % n;
     return r < 0 ? r + n : r;
@@ -264,7 +270,7 @@ __device__ __forceinline__ long long horner_bal(const uint32_t (&b)[ORD]) {
     v += (unsigned long long)(b[1] * 64u + b[0] * 16384u) << 32;
     // (Acc_6 * 256 + Acc_7 + 512) >> 10, the biases folded into one constant
     const int lo = (int)(b[6] * 256u + b[7] + (512u - 257u * 0x4B400000u)) >> 10;
-    return (long long)(v - kBias) + (long long)lo;
+    return (long long)(v + (unsigned long long)(long long)lo + (0ull - kBias));
 }
 
 // FP32 bits -> FP64 value, integer only (normal, zero, subnormal flushed, inf/nan).
@@ -456,7 +462,9 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
     const long long ntiles = BATCH ? prefix[nsweeps]
                                    : ((long long)S0.nL * S0.nR + kM - 1) / kM *
                                          ((S0.qhi - S0.qlo + G::QP) / G::QP) * S0.narr;
-    const int kneed = NCH * (G::QP + NT - 1);         // input elements the tile's outputs use
+    // window offset of the convolution sweeps (0 in batched launches)
+    const int woff = (!BATCH && KIND == KCONV) ? S0.woff : 0;
+    const int kneed = NCH * (G::QP + NT - 1) + woff;  // window elements the tile's outputs use
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
@@ -479,7 +487,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
     for (int idx = tid; idx < G::ND * 16 * G::KB; idx += kThreads) {
         const int t = idx / (16 * G::KB), rem = idx % (16 * G::KB);
         const int n = rem / G::KB, kk = rem % G::KB;
-        const int ti = kk / NCH - n / NCH;
+        const int ti = kk / NCH - n / NCH - woff;
         const uint32_t v = (ti >= 0 && ti < NT) ? F.dig[t][filter_index<KIND>(n % NCH, kk % NCH) * NT + ti] : 0u;
         const int row = 16 * t + n;                      // stacked filter planes
         uint8_t *b = B + (kk / G::CE) * G::LBO_B + (row >> 3) * 128 + (row & 7) * 16 +
@@ -520,7 +528,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             const uint32_t nlines = (uint32_t)S.nL * (uint32_t)S.nR;
             const int plast = S.qhi + S.lowfil + NT - 1;                // last input position used
             const long long in_ext = S.in_ext;
-            const int p0 = S.qlo + loc.ch * G::QP + S.lowfil;           // first input position
+            const int p0 = S.qlo + loc.ch * G::QP + S.lowfil - woff;    // window start position
             const int pstart = S.bc == BC_PERIODIC ? imod(p0, S.n) : 0;
             const bool onewrap = S.n >= G::KT;
             // element kk of the tile -> offset (in elements) in the line, -1 for a zero
@@ -549,15 +557,66 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             const long long stride = S.nL;
             const int klim = min(kneed, NCH * (plast - p0 + 1));
             // the 8 elements of group gi.  The group's first cnt elements are
-            // used (the same for every row of the tile); when their line
-            // offsets are one consecutive run (inside the line, no wrap) they
-            // are loaded from one pointer -- 16-byte vectors along contiguous
-            // lines -- else element by element
+            // used (the same for every row of the tile).  Periodic
+            // convolution lines (the common case) take their positions as at
+            // most two runs (before and after the wrap): contiguous lines by
+            // 32- or 16-byte vectors when the group is one aligned run,
+            // strided lines by one pointer stepping the stride.  Other
+            // boundaries: one pointer when the group's line offsets are one
+            // consecutive run, else element by element.
             auto load8 = [&](int gi, long long (&bits)[8]) {
                 const int i0 = gi * 8;
                 const int cnt = max(0, min(8, klim - i0));
+#pragma unroll
+                for (int e = 0; e < 8; ++e) bits[e] = 0ll;
+                if (cnt <= 0 || !valid) return;
+                if (KIND == KCONV && S.bc == BC_PERIODIC && onewrap) {
+                    int ps0 = pstart + i0;                           // < 2n
+                    if (ps0 >= S.n) ps0 -= S.n;
+                    const int w = S.n - ps0;                         // elements before the wrap
+                    if (stride == 1) {
+                        const long long *q = base + ps0;
+                        if (cnt == 8 && w >= 8) {
+                            if ((((uintptr_t)q) & 31) == 0) {
+                                ld256(q, bits[0], bits[1], bits[2], bits[3]);
+                                ld256(q + 4, bits[4], bits[5], bits[6], bits[7]);
+                                return;
+                            }
+                            if ((((uintptr_t)q) & 15) == 0) {
+                                const double2 *v = reinterpret_cast<const double2 *>(q);
+#pragma unroll
+                                for (int e = 0; e < 4; ++e) {
+                                    const double2 t = v[e];
+                                    bits[2 * e] = __double_as_longlong(t.x);
+                                    bits[2 * e + 1] = __double_as_longlong(t.y);
+                                }
+                                return;
+                            }
+                        }
+#pragma unroll
+                        for (int e = 0; e < 8; ++e)
+                            if (e < cnt) bits[e] = e < w ? q[e] : base[e - w];
+                    } else {
+                        const long long *q = base + (long long)ps0 * stride;
+                        if (cnt == 8 && w >= 8) {
+#pragma unroll
+                            for (int e = 0; e < 8; ++e) {
+                                bits[e] = *q;
+                                q += stride;
+                            }
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < 8; ++e) {
+                                if (e == w) q = base;
+                                if (e < cnt) bits[e] = *q;
+                                q += stride;
+                            }
+                        }
+                    }
+                    return;
+                }
                 long long oa = -1;
-                if (KIND != KREC && cnt > 0) {
+                if (KIND != KREC) {
                     const long long a0 = off_of(i0);
                     if (a0 >= 0 && off_of(i0 + cnt - 1) == a0 + cnt - 1) oa = a0;
                 }
@@ -567,27 +626,26 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                         const double2 *v = reinterpret_cast<const double2 *>(q);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
-                            if (valid && 2 * e + 1 < cnt) {
+                            if (2 * e + 1 < cnt) {
                                 const double2 t = v[e];
                                 bits[2 * e] = __double_as_longlong(t.x);
                                 bits[2 * e + 1] = __double_as_longlong(t.y);
-                            } else {
-                                bits[2 * e] = (valid && 2 * e < cnt) ? q[2 * e] : 0ll;
-                                bits[2 * e + 1] = 0ll;
+                            } else if (2 * e < cnt) {
+                                bits[2 * e] = q[2 * e];
                             }
                         }
                     } else {
 #pragma unroll
                         for (int e = 0; e < 8; ++e) {
-                            bits[e] = (valid && e < cnt) ? *q : 0ll;
+                            if (e < cnt) bits[e] = *q;
                             q += stride;
                         }
                     }
                 } else {
 #pragma unroll
                     for (int e = 0; e < 8; ++e) {
-                        const long long o = (valid && e < cnt) ? off_of(i0 + e) : -1;
-                        bits[e] = o >= 0 ? base[o * stride] : 0ll;
+                        const long long o = e < cnt ? off_of(i0 + e) : -1;
+                        if (o >= 0) bits[e] = base[o * stride];
                     }
                 }
             };
@@ -867,6 +925,11 @@ cudaError_t launch(const Sweep &S_in, const TcFilter &F, int *status, const int 
     using G = Geom<KIND, NT, SCH>;
     Sweep S = S_in;
     if (!tc_prepare(S)) return cudaErrorInvalidValue;
+    // contiguous periodic lines of a filter whose K blocks leave room: start
+    // the window on a 4-element boundary (32-byte aligned groups)
+    if (KIND == KCONV && G::KB - 15 - NT >= 3 && S.nL == 1 && S.bc == BC_PERIODIC && S.n % 4 == 0 &&
+        S.in_ext % 4 == 0 && S.x_arr % 4 == 0 && (((uintptr_t)S.x) & 31) == 0)
+        S.woff = ((S.qlo + S.lowfil) % 4 + 4) % 4;
     cudaError_t e = set_smem_attr<KIND, NT, SCH, false>();
     if (e != cudaSuccess) return e;
     const long long tiles = tile_count_for(S, G::QP);
