@@ -801,6 +801,8 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             const double *const xrow = xa + l + (long long)S.nL * S.in_ext * rr;
             const int se = Er + F.ef - 58;
             const bool nanrow = SCH == SCH_EXACT && Er == 0x7FFFFFFF;
+            // no dot, a_x or a_y term: every output is its value (plus x2), stored
+            const bool lean = KIND == KCONV && !(!BATCH && S.has_dot) && !S.has_ax && S.ay_mode == 0;
 #pragma unroll 1
             for (int step = 0; step < 4; ++step) {             // 2 blocks x 2 x 8 outputs
                 const int jj = step >> 1, n0 = (step & 1) * 8;
@@ -862,6 +864,16 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                             }
                         }
                         double *yq = ystep + yps * (g0 / NCH);   // position of output g0
+                        if (lean && nv >= 8) {
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) {
+                                double out = outv[i];
+                                if (x2) out += add[g0 + i];
+                                *yq = out;
+                                yq += yps;
+                            }
+                            continue;
+                        }
 #pragma unroll
                         for (int i = 0; i < 4; ++i) {
                             const int n = g0 + i;
