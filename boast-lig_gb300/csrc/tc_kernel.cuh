@@ -87,16 +87,24 @@ template <int KIND, int NT, int SCH> struct Geom {
     static constexpr int MK = 32 / ESZ;                          // K of one MMA
     static constexpr int ND = SCH == SCH_EXACT ? 8 : SCH == SCH_BF16X3 ? 3 : 2;
     static constexpr int ORD = ND;                               // order accumulators per block
+    // operand planes interleaved along K: the exact scheme keeps its digit
+    // planes in pairs (K index = 2 * element + plane within the pair), so one
+    // byte permute builds both FP16 digits of an element; split schemes one
+    // plane per slice
+    static constexpr int PL = SCH == SCH_EXACT ? 2 : 1;
+    static constexpr int NS = ND / PL;                           // A slices (MMAs per K step)
     static constexpr int BN = 16 * ORD;                          // rows of the stacked filter
     static constexpr int LBO_B = BN * 16;                        // its K-direction chunk stride
-    static constexpr int A_PLANE = kM * KT * ESZ;
-    static constexpr int A_BYTES = ND * A_PLANE;
-    static constexpr int B_BYTES = BN * KB * ESZ;
+    static constexpr int A_SLICE = kM * KT * PL * ESZ;
+    static constexpr int A_BYTES = NS * A_SLICE;
+    static constexpr int KBP = KB * PL;                          // K of a block window
+    static constexpr int B_BYTES = BN * KBP * ESZ;
     static constexpr int AUX = 1024 + 3 * 4 * kM;                // barriers, slots, row exponents
     static constexpr int SMEM = A_BYTES + B_BYTES + AUX + 1024;
     static constexpr int HALF_COLS = 2 * ORD * 16;               // one TMEM half (2 blocks)
     static constexpr uint32_t TMEM_COLS = 2 * HALF_COLS <= 32 ? 32 : 2 * HALF_COLS <= 64 ? 64 : 2 * HALF_COLS <= 128 ? 128 : 2 * HALF_COLS <= 256 ? 256 : 512;
     static_assert(2 * HALF_COLS <= 512, "TMEM columns");
+    static_assert(ND % PL == 0, "plane slices");
     static_assert(SMEM <= 232448, "shared memory");
     // Instruction descriptor (kind::f16 / kind::tf32): D F32; A and B F16
     // (exact), BF16 or TF32 (formats 0, 1, 2); both K-major; M = 128; N is
@@ -301,17 +309,16 @@ __device__ __forceinline__ void fixed_bal(long long bits, int mx, uint32_t &ul, 
     uh = (uint32_t)(U >> 32);
 }
 
-// FP16 pair of balanced digit b (0 = lowest byte) of two biased fixed points
-// (ul/uh of elements a and b): PRMT gathers the two bytes, 0x6400 makes them
-// 1024 + byte in FP16, one HADD2 subtracts 1024 + 128 (exact).
-__device__ __forceinline__ uint32_t digit_pair_bal(int byte, uint32_t al, uint32_t ah, uint32_t bl,
-                                                   uint32_t bh) {
-    const uint32_t wa = byte >= 4 ? ah : al;
-    const uint32_t wb = byte >= 4 ? bh : bl;
-    const uint32_t sel = (uint32_t)(byte & 3) | ((uint32_t)(4 + (byte & 3)) << 8);   // bytes 0, 2
+// FP16 pair of balanced digits 2p, 2p+1 (bytes 7-2p and 6-2p) of one biased
+// fixed point (ul/uh): PRMT takes the two bytes with a 0x64 byte above each,
+// which makes them 1024 + byte in FP16, and one HADD2 subtracts 1024 + 128
+// (exact).  The lower half is plane 2p (the more significant digit).
+__device__ __forceinline__ uint32_t digit_pair_elem(int p, uint32_t ul, uint32_t uh) {
+    const uint32_t w = p < 2 ? uh : ul;
+    // bytes (3, 2) of the word for even p, (1, 0) for odd p; selector 4 = 0x64
+    const uint32_t sel = (p & 1) ? 0x4041u : 0x4243u;
     uint32_t t;
-    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(t) : "r"(wa), "r"(wb), "r"(sel));
-    t = (t & 0x00FF00FFu) | 0x64006400u;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(t) : "r"(w), "r"(0x64646464u), "r"(sel));
     const uint32_t off = 0xE480E480u;                            // (-1152, -1152) in FP16
     __half2 h = __hadd2(*reinterpret_cast<__half2 *>(&t), *reinterpret_cast<const __half2 *>(&off));
     return *reinterpret_cast<uint32_t *>(&h);
@@ -360,20 +367,21 @@ template <int KIND, int NT, int SCH, int H>
 __device__ __forceinline__ void issue_half(uint32_t tmem, uint64_t a_desc0, uint64_t b_desc0) {
     using G = Geom<KIND, NT, SCH>;
     constexpr bool TF = SCH == SCH_TF32X3;
-    constexpr int NKS = G::KB / G::MK;
+    constexpr int NKS = G::KBP / G::MK;
 #pragma unroll
     for (int jj = 0; jj < 2; ++jj) {
         const int j = 2 * H + jj;
-        const int a_blk = (16 / G::CE) * j * 2048;
+        const int a_blk = (16 * G::PL / G::CE) * j * 2048;
 #pragma unroll
-        for (int sd = 0; sd < G::ND; ++sd) {
+        for (int sl = 0; sl < G::NS; ++sl) {
+            const int sd = sl * G::PL;                           // first plane (order) of the slice
             const uint32_t d = tmem + (uint32_t)(H * G::HALF_COLS + (jj * G::ORD + sd) * 16);
             const uint32_t id = G::idesc(16 * (G::ORD - sd));
 #pragma unroll
             for (int ks = 0; ks < NKS; ++ks) {
-                const uint64_t ad = a_desc0 + (uint64_t)((sd * G::A_PLANE + a_blk + 2 * ks * 2048) >> 4);
+                const uint64_t ad = a_desc0 + (uint64_t)((sl * G::A_SLICE + a_blk + 2 * ks * 2048) >> 4);
                 const uint64_t bd = b_desc0 + (uint64_t)((2 * ks * G::LBO_B) >> 4);
-                mma<TF>(d, ad, bd, id, (sd == 0 && ks == 0) ? 0u : 1u);
+                mma<TF>(d, ad, bd, id, (sl == 0 && ks == 0) ? 0u : 1u);
             }
         }
     }
@@ -484,14 +492,18 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     // Toeplitz filter tiles B_t[n][kk], K-major core matrices
-    for (int idx = tid; idx < G::ND * 16 * G::KB; idx += kThreads) {
-        const int t = idx / (16 * G::KB), rem = idx % (16 * G::KB);
-        const int n = rem / G::KB, kk = rem % G::KB;
+    for (int idx = tid; idx < G::ORD * 16 * G::KBP; idx += kThreads) {
+        const int t = idx / (16 * G::KBP), rem = idx % (16 * G::KBP);
+        const int n = rem / G::KBP, k2 = rem % G::KBP;
+        // K index k2 = element kk, data plane pj within the slice: the pair
+        // (slice plane pj, filter digit t - pj) lands on order column t
+        const int kk = k2 / G::PL, pj = k2 % G::PL;
         const int ti = kk / NCH - n / NCH - woff;
-        const uint32_t v = (ti >= 0 && ti < NT) ? F.dig[t][filter_index<KIND>(n % NCH, kk % NCH) * NT + ti] : 0u;
+        const uint32_t v = (ti >= 0 && ti < NT && t >= pj)
+                               ? F.dig[t - pj][filter_index<KIND>(n % NCH, kk % NCH) * NT + ti] : 0u;
         const int row = 16 * t + n;                      // stacked filter planes
-        uint8_t *b = B + (kk / G::CE) * G::LBO_B + (row >> 3) * 128 + (row & 7) * 16 +
-                     (kk % G::CE) * G::ESZ;
+        uint8_t *b = B + (k2 / G::CE) * G::LBO_B + (row >> 3) * 128 + (row & 7) * 16 +
+                     (k2 % G::CE) * G::ESZ;
         if (G::ESZ == 4) *(uint32_t *)b = v;
         else *(unsigned short *)b = (unsigned short)v;
     }
@@ -685,19 +697,25 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                     ok = false;
                     break;
                 }
-                // 8 elements = 8 / CE core-matrix chunks of 2048 bytes (128 rows)
-                const int off = group_of(c) * (8 / G::CE) * 2048 + (row >> 3) * 128 + (row & 7) * 16;
+                // 8 elements = 8 PL / CE core-matrix chunks of 2048 bytes (128 rows)
+                const int off = group_of(c) * (8 * G::PL / G::CE) * 2048 + (row >> 3) * 128 + (row & 7) * 16;
                 if (SCH == SCH_EXACT) {
                     uint32_t ul[8], uh[8];
 #pragma unroll
                     for (int e = 0; e < 8; ++e) fixed_bal(bits[e], mxe, ul[e], uh[e]);
+                    // slice p holds digit planes 2p, 2p+1 = bytes 7-2p, 6-2p of
+                    // the biased fixed point: one 16-byte core-matrix row per
+                    // 4 elements
 #pragma unroll
-                    for (int sd = 0; sd < G::ND; ++sd) {
-                        uint32_t wds[4];
+                    for (int sl = 0; sl < G::NS; ++sl) {
 #pragma unroll
-                        for (int w = 0; w < 4; ++w)
-                            wds[w] = digit_pair_bal(7 - sd, ul[2 * w], uh[2 * w], ul[2 * w + 1], uh[2 * w + 1]);
-                        *(uint4 *)(A + sd * G::A_PLANE + off) = make_uint4(wds[0], wds[1], wds[2], wds[3]);
+                        for (int h = 0; h < 2; ++h) {
+                            uint32_t wds[4];
+#pragma unroll
+                            for (int w = 0; w < 4; ++w)
+                                wds[w] = digit_pair_elem(sl, ul[4 * h + w], uh[4 * h + w]);
+                            *(uint4 *)(A + sl * G::A_SLICE + off + h * 2048) = make_uint4(wds[0], wds[1], wds[2], wds[3]);
+                        }
                     }
                 } else if (SCH == SCH_BF16X3) {
                     uint32_t h[8][3];
@@ -708,7 +726,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                         uint32_t wds[4];
 #pragma unroll
                         for (int w = 0; w < 4; ++w) wds[w] = (h[2 * w][sd] >> 16) | (h[2 * w + 1][sd] & 0xFFFF0000u);
-                        *(uint4 *)(A + sd * G::A_PLANE + off) = make_uint4(wds[0], wds[1], wds[2], wds[3]);
+                        *(uint4 *)(A + sd * G::A_SLICE + off) = make_uint4(wds[0], wds[1], wds[2], wds[3]);
                     }
                 } else {
                     uint32_t h[8][2];
@@ -716,8 +734,8 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                     for (int e = 0; e < 8; ++e) split_f32<2, 0xFFFFE000u>(f64_to_f32_bits(bits[e]), h[e]);
 #pragma unroll
                     for (int sd = 0; sd < 2; ++sd) {
-                        *(uint4 *)(A + sd * G::A_PLANE + off) = make_uint4(h[0][sd], h[1][sd], h[2][sd], h[3][sd]);
-                        *(uint4 *)(A + sd * G::A_PLANE + off + 2048) = make_uint4(h[4][sd], h[5][sd], h[6][sd], h[7][sd]);
+                        *(uint4 *)(A + sd * G::A_SLICE + off) = make_uint4(h[0][sd], h[1][sd], h[2][sd], h[3][sd]);
+                        *(uint4 *)(A + sd * G::A_SLICE + off + 2048) = make_uint4(h[4][sd], h[5][sd], h[6][sd], h[7][sd]);
                     }
                 }
 #pragma unroll
@@ -802,7 +820,9 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             const int se = Er + F.ef - 58;
             const bool nanrow = SCH == SCH_EXACT && Er == 0x7FFFFFFF;
             // no dot, a_x or a_y term: every output is its value (plus x2), stored
-            const bool lean = KIND == KCONV && !(!BATCH && S.has_dot) && !S.has_ax && S.ay_mode == 0;
+            // (single-sweep launches: the batched form's tile lookup leaves no
+            // registers for a second store path)
+            const bool lean = !BATCH && KIND == KCONV && !S.has_dot && !S.has_ax && S.ay_mode == 0;
 #pragma unroll 1
             for (int step = 0; step < 4; ++step) {             // 2 blocks x 2 x 8 outputs
                 const int jj = step >> 1, n0 = (step & 1) * 8;
