@@ -173,3 +173,37 @@ def test_two_streams_in_flight_keep_their_own_scratch(pkg, O, mode):
                 assert rel(y1[k].cpu().numpy(), yd) <= TOL, ('sweep', k)
                 assert abs(d1[k].item() - dd.value) <= 1e-12 * abs(dd.value), ('sweep dot', k)
         assert np.abs(ks[k].cpu().numpy() - ko).max() <= 1e-12 * np.abs(ko).max(), ('ekin', k)
+
+
+def test_magicfilter3d_lines_keep_their_own_scale(pkg, O):
+    """Every line of an exact tensor-core sweep is scaled by its own largest
+    exponent.  Lines of the second MagicFilter3D sweep (along axis 1) get
+    magnitudes 2^-40, 1 and 2^40 (the input scaled by its axis-2 index), so a
+    line scaled by another line's exponent would lose up to 80 bits: the
+    second sweep's output (left in w2) must match the oracle's to 1e-13 of
+    each magnitude class, and y overall."""
+    import torch
+    from boast_lig_gb300 import inputs
+    n = [64, 96, 32]
+    narr = 2
+    N = int(np.prod(n))
+    x = inputs.uniform(801, N * narr).reshape(narr, n[2], n[1], n[0])
+    scale = 2.0 ** (40 * (np.arange(n[2]) % 3 - 1))
+    x = (x * scale[None, :, None, None]).ravel()
+    dev = torch.device('cuda:0')
+    xd = torch.from_numpy(x).to(dev)
+    yd = torch.zeros(N * narr, dtype=torch.float64, device=dev)
+    w1 = torch.zeros_like(yd)
+    w2 = torch.zeros_like(yd)
+    with pkg.mode(pkg.MODE_TC_EXACT):
+        pkg.Kernel('d_sfrf_ld_narr').run_dev(3, n, [0, 0, 0], n, n, narr, xd, yd, w1, w2)
+    torch.cuda.synchronize()
+    yo, w1o, w2o = np.zeros(N * narr), np.zeros(N * narr), np.zeros(N * narr)
+    assert O.call('oracle_d_sfrf_ld_narr', 3, n, [0, 0, 0], n, n, narr, x, yo, w1o, w2o) == 0
+    # w2 (after the sweeps along axes 0 and 1) is laid out (i2, q0, q1): axis-2 index fastest
+    g = w2.cpu().numpy().reshape(narr, n[1], n[0], n[2])
+    r = w2o.reshape(narr, n[1], n[0], n[2])
+    for cls in range(3):
+        gc, rc = g[..., cls::3], r[..., cls::3]
+        assert np.abs(gc - rc).max() <= TOL * np.abs(rc).max(), cls
+    assert rel(yd.cpu().numpy(), yo) <= TOL
