@@ -826,20 +826,12 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
 #pragma unroll 1
             for (int step = 0; step < 4; ++step) {             // 2 blocks x 2 x 8 outputs
                 const int jj = step >> 1, n0 = (step & 1) * 8;
-                uint32_t acc[G::ORD][8];
-#pragma unroll
-                for (int k = 0; k < G::ORD; ++k)
-                    tmem_ld8(tmem + ((uint32_t)(lq * 32) << 16) +
-                                 (uint32_t)(hf * G::HALF_COLS + (jj * G::ORD + k) * 16 + n0),
-                             acc[k]);
-                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                if (!valid) continue;
                 const int e0 = 16 * (2 * hf + jj) + n0;         // first output element of the step
                 const int q0 = qc0 + e0 / NCH;                  // e0 is a multiple of 8
                 const int nv = (S.qhi - q0 + 1) * NCH;          // valid elements of the step
-                double *const ystep = yrow + yps * (q0 - S.out_lo);
+                // the x2 partials first, so their loads overlap the TMEM loads
                 double add[8];
-                if (KIND == KCONV && x2) {
+                if (KIND == KCONV && x2 && valid) {
                     const double *xp = x2row + x2s * (q0 - x2lo);
 #pragma unroll
                     for (int n = 0; n < 8; ++n) {
@@ -847,76 +839,78 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                         xp += x2s;
                     }
                 }
-                {
-                    // 4 outputs at a time: their values first (independent,
-                    // branch-free chains; one rare fix-up), then their memory side
+                uint32_t acc[G::ORD][8];
 #pragma unroll
-                    for (int g0 = 0; g0 < 8; g0 += 4) {
-                        if (g0 >= nv) continue;
-                        double outv[4];
-                        if constexpr (SCH == SCH_EXACT) {
-                            bool bad = false;
-                            long long Y[4];
+                for (int k = 0; k < G::ORD; ++k)
+                    tmem_ld8(tmem + ((uint32_t)(lq * 32) << 16) +
+                                 (uint32_t)(hf * G::HALF_COLS + (jj * G::ORD + k) * 16 + n0),
+                             acc[k]);
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (!valid || nv <= 0) continue;
+                double *const ystep = yrow + yps * (q0 - S.out_lo);
+                // the 8 outputs' values first (independent, branch-free chains;
+                // one rare fix-up), then their memory side
+                double outv[8];
+                if constexpr (SCH == SCH_EXACT) {
+                    bool bad = false;
+                    long long Y[8];
 #pragma unroll
-                            for (int i = 0; i < 4; ++i) {
-                                uint32_t bb[G::ORD];
+                    for (int i = 0; i < 8; ++i) {
+                        uint32_t bb[G::ORD];
 #pragma unroll
-                                for (int k = 0; k < G::ORD; ++k) bb[k] = acc_bits(acc[k][g0 + i]);
-                                Y[i] = horner_bal<G::ORD>(bb);
-                            }
-#pragma unroll
-                            for (int i = 0; i < 4; ++i) outv[i] = ll_scaled_fast(Y[i], se, bad);
-                            if (bad) {                    // result not a normal number
-#pragma unroll
-                                for (int i = 0; i < 4; ++i) outv[i] = ll_scaled(Y[i], se);
-                            }
-                            if (nanrow) {
-#pragma unroll
-                                for (int i = 0; i < 4; ++i) outv[i] = __longlong_as_double(0x7FF8000000000000LL);
-                            }
-                        } else {                          // sum of the order accumulators
-#pragma unroll
-                            for (int i = 0; i < 4; ++i) {
-                                float f = __uint_as_float(acc[0][g0 + i]);
-#pragma unroll
-                                for (int k = 1; k < G::ORD; ++k) f += __uint_as_float(acc[k][g0 + i]);
-                                outv[i] = f32_to_f64(__float_as_uint(f));
-                            }
-                        }
-                        double *yq = ystep + yps * (g0 / NCH);   // position of output g0
-                        if (lean && nv >= 8) {
-#pragma unroll
-                            for (int i = 0; i < 4; ++i) {
-                                double out = outv[i];
-                                if (x2) out += add[g0 + i];
-                                *yq = out;
-                                yq += yps;
-                            }
-                            continue;
-                        }
-#pragma unroll
-                        for (int i = 0; i < 4; ++i) {
-                            const int n = g0 + i;
-                            const int q = q0 + n / NCH, c = n % NCH;
-                            if (n >= nv) break;
-                            double out = outv[i];
-                            double *const yp = c ? yq + ycs * c : yq;
-                            if (KIND == KCONV) {
-                                const bool want_dot = !BATCH && S.has_dot;   // batched sweeps have no dot
-                                if ((want_dot || S.has_ax) && (!grow || (q >= 0 && q < S.n))) {
-                                    const int ps = S.bc == BC_PERIODIC ? imod(q, S.n) : q - S.in_lo;
-                                    const double xq = xrow[(long long)S.nL * ps];
-                                    if (want_dot) dot = fma(xq, out, dot);
-                                    if (S.has_ax) out = fma(xq, S.a_x, out);
-                                }
-                                if (x2) out += add[n];
-                            }
-                            if (S.ay_mode == 2) out += *yp;
-                            else if (S.ay_mode == 1) out = fma(S.a_y, *yp, out);
-                            *yp = out;
-                            if (c == NCH - 1) yq += yps;
-                        }
+                        for (int k = 0; k < G::ORD; ++k) bb[k] = acc_bits(acc[k][i]);
+                        Y[i] = horner_bal<G::ORD>(bb);
                     }
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) outv[i] = ll_scaled_fast(Y[i], se, bad);
+                    if (bad) {                    // result not a normal number
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) outv[i] = ll_scaled(Y[i], se);
+                    }
+                    if (nanrow) {
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) outv[i] = __longlong_as_double(0x7FF8000000000000LL);
+                    }
+                } else {                          // sum of the order accumulators
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        float f = __uint_as_float(acc[0][i]);
+#pragma unroll
+                        for (int k = 1; k < G::ORD; ++k) f += __uint_as_float(acc[k][i]);
+                        outv[i] = f32_to_f64(__float_as_uint(f));
+                    }
+                }
+                double *yq = ystep;
+                if (lean && nv >= 8) {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        double out = outv[i];
+                        if (x2) out += add[i];
+                        *yq = out;
+                        yq += yps;
+                    }
+                    continue;
+                }
+#pragma unroll
+                for (int n = 0; n < 8; ++n) {
+                    const int q = q0 + n / NCH, c = n % NCH;
+                    if (n >= nv) break;
+                    double out = outv[n];
+                    double *const yp = c ? yq + ycs * c : yq;
+                    if (KIND == KCONV) {
+                        const bool want_dot = !BATCH && S.has_dot;   // batched sweeps have no dot
+                        if ((want_dot || S.has_ax) && (!grow || (q >= 0 && q < S.n))) {
+                            const int ps = S.bc == BC_PERIODIC ? imod(q, S.n) : q - S.in_lo;
+                            const double xq = xrow[(long long)S.nL * ps];
+                            if (want_dot) dot = fma(xq, out, dot);
+                            if (S.has_ax) out = fma(xq, S.a_x, out);
+                        }
+                        if (x2) out += add[n];
+                    }
+                    if (S.ay_mode == 2) out += *yp;
+                    else if (S.ay_mode == 1) out = fma(S.a_y, *yp, out);
+                    *yp = out;
+                    if (c == NCH - 1) yq += yps;
                 }
             }
             // the whole group has read TMEM half hf: it may be reissued
