@@ -198,6 +198,13 @@ __device__ __forceinline__ void ld256(const long long *p, long long &a, long lon
     asm("ld.global.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p));
 }
 
+// 32 bytes to global memory (a 32-byte aligned address) in one store.
+__device__ __forceinline__ void st256(double *p, double a, double b, double c, double d) {
+    asm volatile("st.global.v4.u64 [%0], {%1, %2, %3, %4};" ::"l"(p), "l"(__double_as_longlong(a)),
+                 "l"(__double_as_longlong(b)), "l"(__double_as_longlong(c)), "l"(__double_as_longlong(d))
+                 : "memory");
+}
+
 __device__ __forceinline__ int imod(int a, int n) {
     int r = a % n;
     return r < 0 ? r + n : r;
@@ -822,7 +829,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             // no dot, a_x or a_y term: every output is its value (plus x2), stored
             // (single-sweep launches: the batched form's tile lookup leaves no
             // registers for a second store path)
-            const bool lean = !BATCH && KIND == KCONV && !S.has_dot && !S.has_ax && S.ay_mode == 0;
+            const bool lean = !BATCH && !S.has_dot && !S.has_ax && S.ay_mode == 0;
 #pragma unroll 1
             for (int step = 0; step < 4; ++step) {             // 2 blocks x 2 x 8 outputs
                 const int jj = step >> 1, n0 = (step & 1) * 8;
@@ -882,12 +889,29 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                 }
                 double *yq = ystep;
                 if (lean && nv >= 8) {
+                    if (KIND == KCONV && x2) {
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        double out = outv[i];
-                        if (x2) out += add[i];
-                        *yq = out;
-                        yq += yps;
+                        for (int i = 0; i < 8; ++i) outv[i] += add[i];
+                    }
+                    // a contiguous output line takes the step's 8 outputs as two
+                    // 32-byte runs: elements 0-7 (convolution; synthesis, whose
+                    // channels interleave), or channel 0 and channel 1 (analysis)
+                    double *const r1 = KIND == KDEC ? ystep + ycs : ystep + 4;
+                    if (ys == 1 && ((((uintptr_t)ystep) | ((uintptr_t)r1)) & 31) == 0) {
+                        if (KIND == KDEC) {
+                            st256(ystep, outv[0], outv[2], outv[4], outv[6]);
+                            st256(r1, outv[1], outv[3], outv[5], outv[7]);
+                        } else {
+                            st256(ystep, outv[0], outv[1], outv[2], outv[3]);
+                            st256(r1, outv[4], outv[5], outv[6], outv[7]);
+                        }
+                    } else {
+#pragma unroll
+                        for (int n = 0; n < 8; ++n) {
+                            const int c = n % NCH;
+                            *(c ? yq + ycs * c : yq) = outv[n];
+                            if (c == NCH - 1) yq += yps;
+                        }
                     }
                     continue;
                 }
