@@ -827,9 +827,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             const int se = Er + F.ef - 58;
             const bool nanrow = SCH == SCH_EXACT && Er == 0x7FFFFFFF;
             // no dot, a_x or a_y term: every output is its value (plus x2), stored
-            // (single-sweep launches: the batched form's tile lookup leaves no
-            // registers for a second store path)
-            const bool lean = !BATCH && !S.has_dot && !S.has_ax && S.ay_mode == 0;
+            const bool lean = !S.has_dot && !S.has_ax && S.ay_mode == 0;
 #pragma unroll 1
             for (int step = 0; step < 4; ++step) {             // 2 blocks x 2 x 8 outputs
                 const int jj = step >> 1, n0 = (step & 1) * 8;
