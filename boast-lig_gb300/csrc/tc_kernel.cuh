@@ -634,6 +634,37 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                     }
                     return;
                 }
+                if (KIND == KREC && S.bc == BC_PERIODIC && S.n * NCH >= G::KT) {
+                    // synthesis input: 4 positions x 2 channels, channel c of
+                    // position ps at ps + in_ext c: two runs of 4, read as
+                    // vectors on contiguous lines, interleaved into the group
+                    int ps0 = pstart + i0 / 2;                       // < 2n
+                    if (ps0 >= S.n) ps0 -= S.n;
+                    const int np = cnt / 2, w = S.n - ps0;           // positions, before the wrap
+                    const long long *qL = base + (long long)ps0 * stride, *qH = qL + in_ext * stride;
+                    if (np == 4 && w >= 4) {
+                        if (stride == 1 && ((((uintptr_t)qL) | ((uintptr_t)qH)) & 31) == 0) {
+                            ld256(qL, bits[0], bits[2], bits[4], bits[6]);
+                            ld256(qH, bits[1], bits[3], bits[5], bits[7]);
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < 4; ++j) {
+                                bits[2 * j] = qL[j * stride];
+                                bits[2 * j + 1] = qH[j * stride];
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            if (j >= np) break;
+                            int ps = ps0 + j;
+                            if (ps >= S.n) ps -= S.n;
+                            bits[2 * j] = base[(long long)ps * stride];
+                            bits[2 * j + 1] = base[((long long)ps + in_ext) * stride];
+                        }
+                    }
+                    return;
+                }
                 long long oa = -1;
                 if (KIND != KREC) {
                     const long long a0 = off_of(i0);
@@ -641,7 +672,10 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                 }
                 if (oa >= 0) {
                     const long long *q = base + oa * stride;
-                    if (stride == 1 && ((((uintptr_t)q) & 15) == 0)) {
+                    if (stride == 1 && cnt == 8 && ((((uintptr_t)q) & 31) == 0)) {
+                        ld256(q, bits[0], bits[1], bits[2], bits[3]);
+                        ld256(q + 4, bits[4], bits[5], bits[6], bits[7]);
+                    } else if (stride == 1 && ((((uintptr_t)q) & 15) == 0)) {
                         const double2 *v = reinterpret_cast<const double2 *>(q);
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {

@@ -98,6 +98,23 @@ def test_wavelet1d_all_bcs_shapes(pkg, O, op, bc, idim):
         assert rel(yg, yo) <= TOL, (op, bc, idim, a, ay)
 
 
+@pytest.mark.parametrize('op', WAV_OPS)
+@pytest.mark.parametrize('nproc', [41, 44, 46])
+@pytest.mark.parametrize('idim', [0, 1, 2])
+def test_wavelet1d_periodic_long_lines(pkg, O, op, nproc, idim):
+    """Periodic lines of 41-46 positions (two channels each): a tile's window
+    wraps once, and with lengths not a multiple of 4 the wrap falls inside
+    the 4-position groups the sweeps load as runs."""
+    n = [6, 5, 3]
+    n[idim] = nproc
+    narr = 2
+    s = 8 * int(np.prod(n)) * narr
+    x = seeded(500 + idim, s)
+    y = seeded(600 + idim, s)
+    yg, yo = run_both(pkg, O, op, (3, idim, n, 0, n, n, narr, x, y, 1.0, 0.0), s)
+    assert rel(yg, yo) <= TOL, (op, nproc, idim)
+
+
 @pytest.mark.parametrize('bc', [0, 1, -1, 2])
 @pytest.mark.parametrize('idim', [0, 1, 2])
 def test_kinetic1d_dotin(pkg, O, bc, idim):
