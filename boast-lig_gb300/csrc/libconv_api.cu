@@ -8,6 +8,7 @@
 //    (MagicFilter, wavelets) and transpose = 0 with the kinetic options.
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -24,13 +25,33 @@ using namespace lcg;
 
 namespace {
 
-thread_local std::string t_err;
-thread_local int t_mode = LIBCONV_MODE_FP64;
-
 bool valid_mode(int m) {
     return m == LIBCONV_MODE_FP64 || m == LIBCONV_MODE_TC_EXACT || m == LIBCONV_MODE_TC_BF16X3 ||
            m == LIBCONV_MODE_TC_TF32X3;
 }
+
+// The mode a thread starts in: $LIBCONV_GB300_MODE (fp64, tc_exact, tc_bf16x3,
+// tc_tf32x3, or the number of one of them), read once per process, so callers
+// of the generated procedures can select the tensor-core sweeps without a
+// code change; FP64 when it is unset or names no mode.
+int initial_mode() {
+    static const int m = [] {
+        const char *e = getenv("LIBCONV_GB300_MODE");
+        if (!e) return LIBCONV_MODE_FP64;
+        static const struct { const char *name; int mode; } names[] = {
+            {"fp64", LIBCONV_MODE_FP64}, {"tc_exact", LIBCONV_MODE_TC_EXACT},
+            {"tc_bf16x3", LIBCONV_MODE_TC_BF16X3}, {"tc_tf32x3", LIBCONV_MODE_TC_TF32X3}};
+        for (const auto &n : names)
+            if (strcmp(e, n.name) == 0) return n.mode;
+        char *end = nullptr;
+        const long v = strtol(e, &end, 10);
+        return (end != e && *end == '\0' && valid_mode((int)v)) ? (int)v : LIBCONV_MODE_FP64;
+    }();
+    return m;
+}
+
+thread_local std::string t_err;
+thread_local int t_mode = initial_mode();
 
 int fail(int code, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
 int fail(int code, const char *fmt, ...) {

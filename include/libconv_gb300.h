@@ -59,7 +59,11 @@ extern "C" {
 
 /* Compute modes for libconv_gb300_set_mode (per calling thread).  The
  * tensor-core modes cover every sweep (MagicFilter, kinetic, derivative,
- * wavelet and combined wavelet-MagicFilter filters).
+ * wavelet and combined wavelet-MagicFilter filters).  A thread starts in the
+ * mode named by the environment variable LIBCONV_GB300_MODE (fp64, tc_exact,
+ * tc_bf16x3, tc_tf32x3 or its number, read once per process), so callers of
+ * the generated procedures can select a mode without a code change; in FP64
+ * when the variable is unset or names no mode.
  *   FP64:      plain FP64 FMA kernels on the CUDA cores (default).
  *   TC_EXACT:  tcgen05 tensor cores with exact integer digit arithmetic (FP16
  *              byte digits, FP32 accumulation kept exact); FP64-class accuracy.

@@ -3,6 +3,7 @@ header declares, validates arguments before touching the device, and its
 cost model follows the reference formula (GenericConvolution2.rb:1269-1276,
 1525-1558, 1850-1932)."""
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -56,6 +57,29 @@ def test_mode_setting(pkg):
     pkg.set_mode(pkg.MODE_FP64)
     with pytest.raises(pkg.LibconvError):
         pkg.set_mode(99)
+
+
+@pytest.mark.parametrize('value,mode', [(None, 0), ('tc_exact', 1), ('tc_bf16x3', 2), ('3', 3),
+                                        ('fp64', 0), ('no-such-mode', 0), ('7', 0)])
+def test_initial_mode_from_environment(pkg, value, mode):
+    """A fresh process (and each of its threads) starts in the mode that
+    LIBCONV_GB300_MODE names, FP64 when it is unset or names no mode."""
+    import subprocess
+    import sys
+    env = dict(os.environ)
+    env.pop('LIBCONV_GB300_MODE', None)
+    if value is not None:
+        env['LIBCONV_GB300_MODE'] = value
+    code = ('import ctypes, sys, threading\n'
+            'L = ctypes.CDLL(sys.argv[1])\n'
+            'out = [L.libconv_gb300_get_mode()]\n'
+            't = threading.Thread(target=lambda: out.append(L.libconv_gb300_get_mode()))\n'
+            't.start(); t.join()\n'
+            'print(out[0], out[1])\n')
+    r = subprocess.run([sys.executable, '-c', code, pkg.LIB_PATH], capture_output=True, text=True,
+                       env=env, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.split() == [str(mode), str(mode)]
 
 
 def test_cost_model(pkg):
