@@ -296,7 +296,9 @@ int apply_A(int n, int nsys, const double a[3], const double *eps, const double 
             const double *r_for_pr = nullptr, double *part_pr = nullptr,
             const int *active = nullptr) {
     const int dims[3] = {n, n, n}, bc[3] = {0, 0, 0};
-    int rc = d_kin_narr_dev(3, dims, bc, nsys, x, Tx, w1, w2, a, 0.0, 0.0, st);
+    // converged systems (active[s] == 0) are left out of the sweeps
+    int rc = active ? lcg::kin_narr_active_dev(3, dims, bc, nsys, x, Tx, w1, w2, a, active, st)
+                    : d_kin_narr_dev(3, dims, bc, nsys, x, Tx, w1, w2, a, 0.0, 0.0, st);
     if (rc) return rc;
     const long long N = (long long)n * n * n;
     k_shift<<<dim3(kBPS, nsys), kThreads, 0, st>>>(Tx, x, eps, y, r_for_pr, part, part_pr, N, active);

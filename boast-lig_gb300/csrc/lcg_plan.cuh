@@ -27,6 +27,7 @@ struct Plan {
     int ndot = 1;                     // dot outputs (one per kinetic direction for ekin)
     int exp3[4] = {0, 0, 0, 0};       // n0, n1, n2, narr of the x grid whose line exponents
                                       // the exact tensor-core steps share (0: none)
+    const int *active = nullptr;      // device flags per array: 0 = skip it (no dot plans)
 };
 
 // 3D MagicFilter (sfrf_ld_narr, one grid).  order == nullptr: the reference's
@@ -66,5 +67,9 @@ double *host_staging(size_t bytes, cudaStream_t &st, int &rc);
 int host_finish(cudaStream_t st);
 int report(int code, const char *msg);
 int report_cuda(cudaError_t e, const char *what);
+// d_kin_narr_dev over the arrays a with active[a] != 0 (device flags, read by
+// the kernels on `st`): the other arrays' y is left as it is.
+int kin_narr_active_dev(int d, const int *n, const int *bc, int narr, const double *x, double *y,
+                        double *w1, double *w2, const double *a, const int *active, cudaStream_t st);
 
 }  // namespace lcg

@@ -39,6 +39,9 @@ struct Sweep {
     // elements before the first input position, so that along contiguous
     // lines its 8-element groups start on 32-byte boundaries (0 otherwise)
     int woff = 0;
+    // per array: 0 = skip the array's lines (its output is left as it is); null:
+    // every array (sweeps without a dot product only)
+    const int *active = nullptr;
 };
 
 // Number of dot partials the FP64 sweep writes for S (grid size).

@@ -43,9 +43,10 @@ cudaError_t launch_sweep_tc(const Sweep &S, const TcFilter &F, int sch, int *sta
                             cudaStream_t st, bool lineE_ready = false);
 // Line exponents of narr n0 x n1 x n2 grids along all three axes in one read
 // of x (e0: n1 n2 narr, e1: n0 n2 narr, e2: n0 n1 narr ints), in the line
-// order of the non-rotating sweeps along axes 0, 1, 2.
+// order of the non-rotating sweeps along axes 0, 1, 2.  active (or null):
+// grids with active[a] == 0 are skipped (their entries stay 0).
 cudaError_t launch_line_exp3(const double *x, int n0, int n1, int n2, int narr, int *e0, int *e1,
-                             int *e2, cudaStream_t st);
+                             int *e2, cudaStream_t st, const int *active = nullptr);
 long long sweep_tc_lines(const Sweep &S);
 // Tiles of one sweep (the unit a batched launch numbers consecutively).
 long long sweep_tc_tiles(const Sweep &S);

@@ -469,11 +469,13 @@ int run_plan(const Plan &P, double *const bufs[4], const Scratch &sc, double *do
         exp_off[2] = exp_off[1] + n0 * n2 * na;
         shared_exp = sc.le;
         cudaError_t e = launch_line_exp3(bufs[B_X], (int)n0, (int)n1, (int)n2, (int)na, shared_exp,
-                                         shared_exp + exp_off[1], shared_exp + exp_off[2], st);
+                                         shared_exp + exp_off[1], shared_exp + exp_off[2], st, P.active);
         if (e != cudaSuccess) return cuda_fail(e, "line exponent launch");
     }
+    if (P.active && P.has_dot) return fail(LIBCONV_EARG, "internal: active arrays with a dot product");
     for (const PlanStep &ps : P.steps) {
         Sweep S = ps.S;
+        S.active = P.active;
         S.x = bufs[ps.src];
         S.y = bufs[ps.dst];
         S.x2 = ps.src2 >= 0 ? bufs[ps.src2] : nullptr;
@@ -1196,6 +1198,14 @@ int plan_kinetic(int d, const int *n, const int *bc, const double *a, double a_x
 }
 const double *filter_table() { return h_ftab; }
 int current_mode() { return t_mode; }
+int kin_narr_active_dev(int d, const int *n, const int *bc, int narr, const double *x, double *y,
+                        double *w1, double *w2, const double *a, const int *active, cudaStream_t st) {
+    Plan P;
+    int rc = plan_kin(d, n, bc, a, 0.0, 0.0, P, narr);
+    if (rc) return rc;
+    P.active = active;
+    return exec_dev(P, x, y, w1, w2, nullptr, st);
+}
 int *device_status(int &rc) {
     std::lock_guard<std::recursive_mutex> lk(g_mu);
     DevState *s = dev_state(rc);

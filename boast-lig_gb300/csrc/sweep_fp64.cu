@@ -172,6 +172,7 @@ __global__ void __launch_bounds__(kThreads) sweep_fp64_kernel(const __grid_const
     constexpr int NROW = (QC + NT - 1) * (KIND == KCONV ? 1 : 2);
     __shared__ double tile[NROW * kPad];
     __shared__ double red[kWarps];
+    if (S.active && !S.active[blockIdx.z]) return;          // array skipped (no dot here)
     const long long b = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
     sweep_block<KIND, NT, QC>(S, blockIdx.x, blockIdx.y, blockIdx.z, tile, red, b);
 }

@@ -106,11 +106,13 @@ __global__ void line_exp_batch_kernel(const Sweep *__restrict__ descs, int *out)
 constexpr int kExpChunk = 8;
 __global__ void __launch_bounds__(256)
 line_exp3_kernel(const double *__restrict__ x, int n0, int n1, int n2, int nseg,
-                 int *__restrict__ e0, int *__restrict__ e1, int *__restrict__ e2) {
+                 int *__restrict__ e0, int *__restrict__ e1, int *__restrict__ e2,
+                 const int *__restrict__ active) {
     __shared__ int ys[kExpChunk][8][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int i0 = blockIdx.x * 32 + tx, i1 = blockIdx.y * 8 + ty;
     const long long a = blockIdx.z / nseg;
+    if (active && !active[a]) return;                   // grid skipped (uniform over the block)
     const int seg = blockIdx.z % nseg, seglen = (n2 + nseg - 1) / nseg;
     const int zb = seg * seglen, ze = min(n2, zb + seglen);
     const bool valid = i0 < n0 && i1 < n1;
@@ -164,7 +166,7 @@ constexpr int kExpChunkHost = tck::kExpChunk;
 long long sweep_tc_lines(const Sweep &S) { return (long long)S.nL * S.nR * S.narr; }
 
 cudaError_t launch_line_exp3(const double *x, int n0, int n1, int n2, int narr, int *e0, int *e1,
-                             int *e2, cudaStream_t st) {
+                             int *e2, cudaStream_t st, const int *active) {
     if (n0 < 1 || n1 < 1 || n2 < 1 || narr < 1 || narr > 65535) return cudaErrorInvalidValue;
     const long long gx = (n0 + 31) / 32, gy = (n1 + 7) / 8;
     // segments of i2 so that a few grids still give the GPU about 8 blocks per SM
@@ -180,7 +182,7 @@ cudaError_t launch_line_exp3(const double *x, int n0, int n1, int n2, int narr, 
         e = cudaMemsetAsync(e2, 0, (size_t)n0 * n1 * narr * sizeof(int), st);
     if (e != cudaSuccess) return e;
     dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)(narr * nseg));
-    tck::line_exp3_kernel<<<grid, 256, 0, st>>>(x, n0, n1, n2, (int)nseg, e0, e1, e2);
+    tck::line_exp3_kernel<<<grid, 256, 0, st>>>(x, n0, n1, n2, (int)nseg, e0, e1, e2, active);
     return cudaGetLastError();
 }
 

@@ -540,9 +540,10 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
         auto group_of = [&](int c) -> int {          // c-th group of this thread
             return c < 2 ? 2 * half + c : c < 4 ? 4 + 2 * half + (c - 2) : 8 + G2 * half + (c - 4);
         };
-        uint32_t it = 0;
-        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+        uint32_t it = 0;                                  // tiles processed (inactive arrays skipped)
+        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
             const TileLoc loc = locate<BATCH>(S0, descs, prefix, nsweeps, tile);
+            if (!BATCH && S0.active && !S0.active[loc.arr]) continue;
             const Sweep &S = *loc.S;
             const uint32_t nlines = (uint32_t)S.nL * (uint32_t)S.nR;
             const int plast = S.qhi + S.lowfil + NT - 1;                // last input position used
@@ -788,6 +789,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                 }
             }
             if (!ok) { alive = false; break; }
+            ++it;
         }
     } else {
         // ============ epilogue: warp group hf issues and drains TMEM half hf
@@ -806,8 +808,10 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             if (lane == 0) S0.dot_part[((long long)dot_arr * gridDim.x + blockIdx.x) * 8 + ew] = dot;
             dot = 0.0;
         };
-        uint32_t it = 0;
-        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+        uint32_t it = 0;                                  // tiles processed (inactive arrays skipped)
+        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+            if (!BATCH && S0.active && !S0.active[locate<BATCH>(S0, descs, prefix, nsweeps, tile).arr])
+                continue;                                 // the producers skip the same tiles
             // the group issues its TMEM half's MMAs for this tile (the half was
             // drained by the group at the end of the previous tile) once the
             // chunk pairs they read are written: half 0 pairs 0-1, half 1 pairs 1-2
@@ -973,6 +977,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
             bar_arrive(gsync[hf]);
             if (!bar_wait(gsync[hf], it & 1)) { alive = false; break; }
+            ++it;
         }
         if (!BATCH && S0.has_dot && dot_arr >= 0) flush_dot();
     }
