@@ -422,8 +422,85 @@ WORKLOADS = {'mfkin128': MfKin128(), 'wavelet96': Wavelet96(), 'orbitals512': Or
              'poisson256': Poisson256()}
 
 
+def gpu_uuid(dev):
+    """'GPU-<uuid>' of CUDA device dev (the name NVML and nvidia-smi -i
+    accept whatever devices CUDA_VISIBLE_DEVICES hides or renumbers), or None."""
+    try:
+        import torch
+        u = getattr(torch.cuda.get_device_properties(dev), 'uuid', None)
+        return None if u is None else 'GPU-' + str(u)
+    except Exception:
+        return None
+
+
+class NvmlClocks:
+    """Read-only NVML sampler (ctypes on the driver's libnvidia-ml): the SM
+    clock and the clock-event reasons of one GPU every `period` seconds in a
+    background thread, so that a timed region shorter than nvidia-smi's
+    sampling interval still gets a clock record.  Settings are only read."""
+    SM = 1                                             # NVML_CLOCK_SM
+    BITS = {0x8: 'hw_slowdown', 0x40: 'hw_thermal_slowdown', 0x20: 'sw_thermal_slowdown',
+            0x4: 'sw_power_cap'}
+
+    def __init__(self, dev, period=0.005):
+        import ctypes
+        import threading
+        self.ok = False
+        self.samples = []
+        self.period = period
+        self.stop_ev = threading.Event()
+        self.th = None
+        try:
+            L = ctypes.CDLL('libnvidia-ml.so.1')
+            if L.nvmlInit_v2() != 0:
+                return
+            h = ctypes.c_void_p()
+            uid = gpu_uuid(dev)
+            if uid is not None:
+                if L.nvmlDeviceGetHandleByUUID(ctypes.c_char_p(uid.encode()), ctypes.byref(h)) != 0:
+                    return
+            elif L.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(dev), ctypes.byref(h)) != 0:
+                return
+            reasons = getattr(L, 'nvmlDeviceGetCurrentClocksEventReasons', None) or \
+                L.nvmlDeviceGetCurrentClocksThrottleReasons
+            mx = ctypes.c_uint(0)
+            L.nvmlDeviceGetMaxClockInfo(h, self.SM, ctypes.byref(mx))
+            self.L, self.h, self.reasons, self.max_mhz = L, h, reasons, mx.value
+            self.ok = True
+        except (OSError, AttributeError):
+            self.ok = False
+
+    def _run(self):
+        import ctypes
+        mhz, bits = ctypes.c_uint(0), ctypes.c_ulonglong(0)
+        while not self.stop_ev.is_set():
+            if (self.L.nvmlDeviceGetClockInfo(self.h, self.SM, ctypes.byref(mhz)) == 0 and
+                    self.reasons(self.h, ctypes.byref(bits)) == 0):
+                self.samples.append((mhz.value, bits.value))
+            self.stop_ev.wait(self.period)
+
+    def start(self):
+        if self.ok:
+            import threading
+            self.th = threading.Thread(target=self._run, daemon=True)
+            self.th.start()
+
+    def stop(self):
+        if not self.th:
+            return None
+        self.stop_ev.set()
+        self.th.join()
+        if not self.samples:
+            return None
+        reasons = sorted({n for _, b in self.samples for bit, n in self.BITS.items() if b & bit})
+        return {'sm_mhz': float(np.median([m for m, _ in self.samples])),
+                'sm_max_mhz': float(self.max_mhz) if self.max_mhz else None,
+                'reasons': reasons, 'samples': len(self.samples)}
+
+
 class Clocks:
-    """nvidia-smi sampler running during the timed region."""
+    """Clock record of the timed region: NVML sampled every 5 ms when the
+    driver's library loads, with nvidia-smi (200 ms) running beside it."""
     Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
          'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
          'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
@@ -432,34 +509,44 @@ class Clocks:
         self.dev = dev
         self.p = None
         self.out = os.path.join('/tmp', f'lcg_clocks_{os.getpid()}.csv')
+        self.nvml = NvmlClocks(dev)
 
     def start(self):
+        self.nvml.start()
         try:
-            self.p = subprocess.Popen(['nvidia-smi', '-i', str(self.dev), f'--query-gpu={self.Q}',
+            self.p = subprocess.Popen(['nvidia-smi', '-i', gpu_uuid(self.dev) or str(self.dev),
+                                       f'--query-gpu={self.Q}',
                                        '--format=csv,noheader,nounits', '-lms', '200'],
                                       stdout=open(self.out, 'w'), stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
 
     def stop(self):
-        if self.p is None:
-            return None
-        time.sleep(0.25)
-        self.p.terminate()
-        self.p.wait()
-        rows = []
-        for line in open(self.out):
-            f = [t.strip() for t in line.split(',')]
-            if len(f) >= 9:
-                rows.append(f)
-        if not rows:
-            return None
-        sm = [float(r[1]) for r in rows if r[1].replace('.', '').isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace('.', '').isdigit()]
-        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
-        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == 'Active'})
-        return {'sm_mhz': float(np.median(sm)) if sm else None,
-                'sm_max_mhz': max(mx) if mx else None, 'reasons': reasons, 'samples': len(rows)}
+        fast = self.nvml.stop()
+        smi = None
+        if self.p is not None:
+            time.sleep(0.25)
+            self.p.terminate()
+            self.p.wait()
+            rows = []
+            for line in open(self.out):
+                f = [t.strip() for t in line.split(',')]
+                if len(f) >= 9:
+                    rows.append(f)
+            if rows:
+                sm = [float(r[1]) for r in rows if r[1].replace('.', '').isdigit()]
+                mx = [float(r[2]) for r in rows if r[2].replace('.', '').isdigit()]
+                names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+                reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == 'Active'})
+                smi = {'sm_mhz': float(np.median(sm)) if sm else None,
+                       'sm_max_mhz': max(mx) if mx else None, 'reasons': reasons, 'samples': len(rows)}
+        if fast:
+            if smi:   # a reason either sampler saw counts
+                fast['reasons'] = sorted(set(fast['reasons']) | set(smi['reasons']))
+                fast['nvidia_smi'] = smi
+            fast['source'] = 'NVML every 5 ms during the timed region (nvidia-smi every 200 ms beside it)'
+            return fast
+        return smi
 
 
 # ----------------------------------------------------------------------------- CPU
