@@ -57,7 +57,9 @@
 //              thread = TMEM lane = tile row; TMEM -> FP64 -> global.
 // Every hand-off is an mbarrier whose phase can never run two phases ahead of
 // its waiter; every wait gives up after ~2 s of SM clock (status word set,
-// TMEM freed, kernel returns).
+// TMEM freed, kernel returns).  In single-sweep launches every role skips the
+// tiles of an array whose S0.active flag is 0 (flags fixed for the launch), so
+// the roles still meet on the same tiles and count only those.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
