@@ -42,6 +42,15 @@ struct Sweep {
     // per array: 0 = skip the array's lines (its output is left as it is); null:
     // every array (sweeps without a dot product only)
     const int *active = nullptr;
+    // exact tensor-core transposed convolution sweeps whose tiles hold whole
+    // lines of the next sweep (run_plan decides): the epilogue writes the
+    // largest exponent field of each of the next sweep's lines,
+    // le_next[a le_next_lines + i2 + le_n2 (q - out_lo)], for this sweep's line
+    // i1 + le_n1 i2 and output q (le_n1 = the next sweep's line length: 32, 64
+    // or 128, so that every tile column covers whole lines)
+    int *le_next = nullptr;
+    long long le_next_lines = 0;
+    int le_n1 = 0, le_n2 = 0;
 };
 
 // Number of dot partials the FP64 sweep writes for S (grid size).

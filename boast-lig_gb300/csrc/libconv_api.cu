@@ -413,6 +413,33 @@ struct Scratch {
 
 // Elements of dot partials and of line exponents that run_plan(P) needs in
 // the calling thread's mode.
+// Exact tensor-core step k hands its successor the line exponents of its
+// output (the epilogue writes them, Sweep::le_next) instead of a pre-pass
+// over that output: k is a periodic transposed convolution with the plain
+// store path (no dot, a_x, a_y or x2) over whole tiles of valid lines, k + 1 a
+// periodic convolution reading k's output along its fastest axis (length n1
+// = 32, 64 or 128, so that every tile column holds whole lines of k + 1: k's
+// line i1 + n1 i2 and output q are k + 1's line i2 + n2 q at position i1).
+bool exp_handoff(const Plan &P, size_t k, int &n1, int &n2) {
+    if (t_mode != LIBCONV_MODE_TC_EXACT || k + 1 >= P.steps.size()) return false;
+    const PlanStep &a = P.steps[k], &b = P.steps[k + 1];
+    const Sweep &A = a.S, &B = b.S;
+    if (!(A.kind == KCONV && A.transpose && A.nL == 1 && A.bc == BC_PERIODIC && !A.has_dot &&
+          !A.has_ax && A.ay_mode == 0 && a.src2 < 0 && sweep_tc_supported(A)))
+        return false;
+    if (!(B.kind == KCONV && B.nL == 1 && B.bc == BC_PERIODIC && b.src == a.dst && b.exp_axis < 0 &&
+          B.narr == A.narr && B.x_arr == A.y_arr && sweep_tc_supported(B)))
+        return false;
+    const long long lines = (long long)A.nL * A.nR;
+    if (!(B.n == 32 || B.n == 64 || B.n == 128) || lines % 128 || lines % B.n) return false;
+    if ((A.qhi - A.qlo + 1) % 64 || A.out_lo != 0 || A.qlo != 0 || B.in_lo != 0 || B.in_ext != B.n)
+        return false;
+    if ((long long)B.nR != lines / B.n * A.out_ext) return false;
+    n1 = B.n;
+    n2 = (int)(lines / B.n);
+    return true;
+}
+
 void plan_scratch(const Plan &P, size_t &ndot, size_t &nle) {
     ndot = nle = 0;
     const bool exact = t_mode == LIBCONV_MODE_TC_EXACT;
@@ -430,6 +457,13 @@ void plan_scratch(const Plan &P, size_t &ndot, size_t &nle) {
         const bool shared = exact && P.exp3[0] > 0 && ps.exp_axis >= 0 && ps.src == B_X;
         if (tc && exact && !shared && (size_t)sweep_tc_lines(S) > nle) nle = (size_t)sweep_tc_lines(S);
     }
+    // a hand-off writes the next step's exponents beside the ones being read
+    int n1, n2;
+    for (size_t k = 0; k + 1 < P.steps.size(); ++k)
+        if (!(P.exp3[0] > 0) && exp_handoff(P, k, n1, n2)) {
+            nle *= 2;
+            break;
+        }
 }
 
 // The host-pointer paths' scratch: their own buffers, grown under the lock
@@ -473,7 +507,18 @@ int run_plan(const Plan &P, double *const bufs[4], const Scratch &sc, double *do
         if (e != cudaSuccess) return cuda_fail(e, "line exponent launch");
     }
     if (P.active && P.has_dot) return fail(LIBCONV_EARG, "internal: active arrays with a dot product");
-    for (const PlanStep &ps : P.steps) {
+    // exponents handed from step to step: the step reads le_cur (ready when the
+    // previous step wrote it) and writes its successor's into the other half
+    int *le_cur = sc.le, *le_other = nullptr;
+    bool le_ready = false;
+    if (!shared_exp) {
+        size_t half = 0;
+        for (const PlanStep &ps : P.steps)
+            if ((size_t)sweep_tc_lines(ps.S) > half) half = (size_t)sweep_tc_lines(ps.S);
+        if (sc.le && sc.nle >= 2 * half) le_other = sc.le + half;
+    }
+    for (size_t k = 0; k < P.steps.size(); ++k) {
+        const PlanStep &ps = P.steps[k];
         Sweep S = ps.S;
         S.active = P.active;
         S.x = bufs[ps.src];
@@ -509,15 +554,29 @@ int run_plan(const Plan &P, double *const bufs[4], const Scratch &sc, double *do
             S.has_a = 0;   // folded into the filter operands
             int *lineE = nullptr;
             const bool shared = sch == SCH_EXACT && shared_exp && ps.exp_axis >= 0 && ps.src == B_X;
+            bool ready = shared, handed = false;
             if (shared) {
                 lineE = shared_exp + exp_off[ps.exp_axis];
             } else if (sch == SCH_EXACT) {
                 if (shared_exp) return fail(LIBCONV_EARG, "plan shares line exponents but a step does not");
-                lineE = sc.le;
+                lineE = le_cur;
+                ready = le_ready;
+                int n1, n2;
+                if (le_other && exp_handoff(P, k, n1, n2)) {
+                    const Sweep &B = P.steps[k + 1].S;
+                    S.le_next = le_other;
+                    S.le_next_lines = (long long)B.nL * B.nR;
+                    S.le_n1 = n1;
+                    S.le_n2 = n2;
+                    handed = true;
+                }
             }
-            e = launch_sweep_tc(S, F, sch, status, lineE, st, shared);
+            e = launch_sweep_tc(S, F, sch, status, lineE, st, ready);
+            if (handed) std::swap(le_cur, le_other);
+            le_ready = handed;
         } else {
             e = launch_sweep_fp64(S, st);
+            le_ready = false;
         }
         if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
         if (S.has_dot) {

@@ -101,7 +101,8 @@ template <int KIND, int NT, int SCH> struct Geom {
     static constexpr int A_BYTES = NS * A_SLICE;
     static constexpr int KBP = KB * PL;                          // K of a block window
     static constexpr int B_BYTES = BN * KBP * ESZ;
-    static constexpr int AUX = 1024 + 3 * 4 * kM;                // barriers, slots, row exponents
+    static constexpr int AUX = 1024 + 3 * 4 * kM + 2 * 4 * 32 * 4;   // barriers, slots, row exponents,
+                                                                 // next-sweep column maxima
     static constexpr int SMEM = A_BYTES + B_BYTES + AUX + 1024;
     static constexpr int HALF_COLS = 2 * ORD * 16;               // one TMEM half (2 blocks)
     static constexpr uint32_t TMEM_COLS = 2 * HALF_COLS <= 32 ? 32 : 2 * HALF_COLS <= 64 ? 64 : 2 * HALF_COLS <= 128 ? 128 : 2 * HALF_COLS <= 256 ? 256 : 512;
@@ -464,6 +465,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
     uint64_t *bars = (uint64_t *)aux;                 // 9 barriers (16 slots)
     uint32_t *tslot = (uint32_t *)(aux + 128);
     int *rowE3 = (int *)(aux + 1024);                 // row exponents, by tile index mod 3
+    int *colE = (int *)(aux + 1024 + 3 * 4 * kM);     // [group][warp][column]: next-sweep line maxima
     // pfull[p]: chunk pair p of the tile is written (producer arrivals);
     // pfree0: pair 0 may be rewritten (the MMAs of TMEM half 0 completed);
     // pfree12: pairs 1 and 2 may be rewritten (both halves' MMAs completed:
@@ -931,6 +933,19 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
 #pragma unroll
                         for (int i = 0; i < 8; ++i) outv[i] += add[i];
                     }
+                    if (!BATCH && KIND == KCONV && S0.le_next) {
+                        // the warp's maximum exponent field of each of the 8 output
+                        // columns (every lane is here: run_plan hands off only
+                        // whole tiles of valid lines); lane i keeps column i's
+                        uint32_t mine = 0;
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            const uint32_t ex = (uint32_t)((unsigned long long)__double_as_longlong(outv[i]) >> 52) & 0x7FFu;
+                            const uint32_t m = __reduce_max_sync(0xffffffffu, ex);
+                            if (lane == i) mine = m;
+                        }
+                        if (lane < 8) colE[(hf * 4 + lq) * 32 + step * 8 + lane] = (int)mine;
+                    }
                     // a contiguous output line takes the step's 8 outputs as two
                     // 32-byte runs: elements 0-7 (convolution; synthesis, whose
                     // channels interleave), or channel 0 and channel 1 (analysis)
@@ -979,6 +994,20 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
             bar_arrive(gsync[hf]);
             if (!bar_wait(gsync[hf], it & 1)) { alive = false; break; }
+            if (!BATCH && KIND == KCONV && S0.le_next && lq == 0) {
+                // lane c: output column 32 hf + c; the tile's 128 lines form 128 / n1
+                // of the next sweep's lines per column, warps (32 lq) / n1 == k the
+                // k-th (the group's other warps wrote colE before the barrier, and
+                // write it again only after this warp issues the next tile's MMAs)
+                const int n1 = S0.le_n1, per = kM / n1;
+                const int q = qc0 + 32 * hf + lane;
+                for (int k = 0; k < per; ++k) {
+                    int m = 0;
+                    for (int w = k * n1 / 32; w < (k + 1) * n1 / 32; ++w) m = max(m, colE[(hf * 4 + w) * 32 + lane]);
+                    const long long i2 = (long long)loc.lb * per + k;
+                    S0.le_next[(long long)arr * S0.le_next_lines + i2 + (long long)S0.le_n2 * (q - S0.out_lo)] = m;
+                }
+            }
             ++it;
         }
         if (!BATCH && S0.has_dot && dot_arr >= 0) flush_dot();

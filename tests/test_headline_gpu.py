@@ -207,3 +207,28 @@ def test_magicfilter3d_lines_keep_their_own_scale(pkg, O):
         gc, rc = g[..., cls::3], r[..., cls::3]
         assert np.abs(gc - rc).max() <= TOL * np.abs(rc).max(), cls
     assert rel(yd.cpu().numpy(), yo) <= TOL
+
+
+@pytest.mark.parametrize('narr', [1, 2])
+def test_magicfilter3d_exponent_handoff_matches_separate_sweeps(pkg, narr):
+    """On 128 x 128 x 32 grids each exact MagicFilter3D sweep hands the next one
+    its line exponents from the epilogue (every tile column holds whole lines
+    of the next sweep: 128 of them after the first sweep, 4 x 32 after the
+    second).  The exact products depend only on each line's exponent, so the
+    result must equal three 1D MagicFilter sweeps, each with its own exponent
+    pass, bit for bit; the input's magnitude steps by 2^40 along axis 2 (every
+    line of the second sweep has its own scale)."""
+    from boast_lig_gb300 import inputs
+    n = [128, 128, 32]
+    N = int(np.prod(n))
+    x = inputs.uniform(907, N * narr).reshape(narr, n[2], n[1], n[0])
+    x = (x * (2.0 ** (40 * (np.arange(n[2]) % 3 - 1)))[None, :, None, None]).ravel()
+    y, w = np.zeros(N * narr), np.zeros(1)
+    t1, t2, t3 = np.zeros(N * narr), np.zeros(N * narr), np.zeros(N * narr)
+    with pkg.mode(pkg.MODE_TC_EXACT):
+        pkg.Kernel('d_sfrf_ld_narr').run(3, n, [0, 0, 0], n, n, narr, x, y, w, w)
+        k = pkg.Kernel('d_s0s0_1d_sym8_md')
+        k.run(3, 0, n, 0, n, n, narr, x, t1, 1.0, 0.0, 0.0)
+        k.run(3, 1, n, 0, n, n, narr, t1, t2, 1.0, 0.0, 0.0)
+        k.run(3, 2, n, 0, n, n, narr, t2, t3, 1.0, 0.0, 0.0)
+    assert np.array_equal(y, t3), float(np.abs(y - t3).max() / np.abs(t3).max())
