@@ -96,8 +96,8 @@ __global__ void line_exp_batch_kernel(const Sweep *__restrict__ descs, int *out)
 // e1[i0 + n0 (i2 + n2 a)] over i1, e2[i0 + n0 (i1 + n1 a)] over i2 -- the
 // line orders of the three non-rotating sweeps of the grid.  Block: 32 i0 x
 // 8 i1 threads over one segment of i2 (blockIdx.z = a nseg + segment), in
-// chunks of 8 planes (8 loads in flight per thread).  e2 is a thread's own
-// maximum; each chunk is staged in shared memory (rows padded to 33 words,
+// chunks of 8 planes (the next chunk's 8 loads in flight while one chunk is
+// reduced).  e2 is a thread's own maximum; each chunk is staged in shared memory (rows padded to 33 words,
 // so the row and the column reads below are free of bank conflicts), where
 // 4 threads per (plane, i1) row reduce the 32 i0 values for e0 and one
 // thread per (plane, i0) column the 8 i1 values for e1.  Partial maxima are
@@ -124,11 +124,17 @@ line_exp3_kernel(const double *__restrict__ x, int n0, int n1, int n2, int nseg,
     const int c0r = row >> 3, r0 = row & 7;
     const int i1r = blockIdx.y * 8 + r0;
     int zmax = 0;
+    // the next chunk's loads are in flight while this chunk is reduced
+    unsigned long long raw[kExpChunk];
+#pragma unroll
+    for (int c = 0; c < kExpChunk; ++c) raw[c] = (valid && zb + c < ze) ? xa[plane * (zb + c)] : 0ull;
     for (int c0 = zb; c0 < ze; c0 += kExpChunk) {
         int e[kExpChunk];
 #pragma unroll
-        for (int c = 0; c < kExpChunk; ++c)
-            e[c] = (valid && c0 + c < ze) ? (int)((xa[plane * (c0 + c)] >> 52) & 0x7FF) : 0;
+        for (int c = 0; c < kExpChunk; ++c) e[c] = (int)((raw[c] >> 52) & 0x7FF);
+        const int c1n = c0 + kExpChunk;
+#pragma unroll
+        for (int c = 0; c < kExpChunk; ++c) raw[c] = (valid && c1n + c < ze) ? xa[plane * (c1n + c)] : 0ull;
 #pragma unroll
         for (int c = 0; c < kExpChunk; ++c) {
             zmax = max(zmax, e[c]);
