@@ -97,10 +97,11 @@ __global__ void line_exp_batch_kernel(const Sweep *__restrict__ descs, int *out)
 // line orders of the three non-rotating sweeps of the grid.  Block: 32 i0 x
 // 8 i1 threads over one segment of i2 (blockIdx.z = a nseg + segment), in
 // chunks of 8 planes (the next chunk's 8 loads in flight while one chunk is
-// reduced).  e2 is a thread's own maximum; each chunk is staged in shared memory (rows padded to 33 words,
-// so the row and the column reads below are free of bank conflicts), where
-// 4 threads per (plane, i1) row reduce the 32 i0 values for e0 and one
-// thread per (plane, i0) column the 8 i1 values for e1.  Partial maxima are
+// reduced).  e2 is a thread's own maximum; each chunk is staged in shared
+// memory (rows padded to 33 words, so the row and the column reads below are
+// free of bank conflicts), where 4 threads per (plane, i1) row reduce the 32
+// i0 values for e0 and one thread per (plane, i0) column the 8 i1 values for
+// e1.  Partial maxima are
 // combined across blocks with atomicMax (e0, e1 and, with several segments,
 // e2 zeroed first).
 constexpr int kExpChunk = 8;
