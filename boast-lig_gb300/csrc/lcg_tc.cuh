@@ -80,6 +80,9 @@ cudaError_t launch_tf32x3(const Sweep &S, const TcFilter &F, int *status, const 
 cudaError_t launch_exact_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
                                int nsweeps, const TcFilter &F, int *status, const int *lineE,
                                cudaStream_t st);
+// Input elements one tile of an exact convolution sweep of ntaps taps reads
+// along each line (a huge value for an unsupported filter length).
+int exact_conv_window(int ntaps);
 cudaError_t launch_bf16x3_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
                                 int nsweeps, const TcFilter &F, int *status, cudaStream_t st);
 cudaError_t launch_tf32x3_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,

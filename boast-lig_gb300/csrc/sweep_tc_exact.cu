@@ -18,6 +18,13 @@ cudaError_t launch_exact(const Sweep &S, const TcFilter &F, int *status, const i
     return cudaErrorInvalidValue;
 }
 
+int exact_conv_window(int ntaps) {
+    if (ntaps == 16) return Geom<KCONV, 16, SCH_EXACT>::KT;
+    if (ntaps == 17) return Geom<KCONV, 17, SCH_EXACT>::KT;
+    if (ntaps == 29) return Geom<KCONV, 29, SCH_EXACT>::KT;
+    return 1 << 30;
+}
+
 cudaError_t launch_exact_batch(int kind, int ntaps, const Sweep *descs, const long long *prefix,
                                int nsweeps, const TcFilter &F, int *status, const int *lineE,
                                cudaStream_t st) {

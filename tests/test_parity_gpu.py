@@ -115,6 +115,32 @@ def test_wavelet1d_periodic_long_lines(pkg, O, op, nproc, idim):
     assert rel(yg, yo) <= TOL, (op, nproc, idim)
 
 
+@pytest.mark.parametrize('op', CONV_OPS)
+@pytest.mark.parametrize('nproc', [80, 97, 130, 203])
+def test_conv1d_periodic_long_contiguous_lines(pkg, O, op, nproc):
+    """Contiguous periodic lines at least one tile window long (80 input
+    elements for 16 taps, 96 for 29): the exact sweep takes each tile
+    window's largest exponent in its producers instead of a pass over the
+    array (80 with 29 taps stays below the window and keeps the pass).
+    Lengths not a multiple of 4 put the wrap inside the 8-element groups.
+    Every line has its own magnitude (2^-40, 1, 2^40) and magnitudes also step
+    by 2^20 along each line, so the tile windows of one line get different
+    scales; each line must match the oracle to 1e-13 of its largest output."""
+    n = [nproc, 6, 5]
+    narr = 2
+    lines = n[1] * n[2] * narr
+    x = seeded(700 + nproc, nproc * lines).reshape(lines, nproc)
+    line_scale = 2.0 ** (40 * (np.arange(lines) % 3 - 1))
+    along = 2.0 ** (20 * ((np.arange(nproc) // 48) % 2))
+    x = (x * line_scale[:, None] * along[None, :]).ravel()
+    for (a, ax, ay) in [(1.0, 0.0, 0.0), (0.7, -0.3, 1.5)]:
+        y = seeded(800 + nproc, x.size)
+        yg, yo = run_both(pkg, O, op, (3, 0, n, 0, n, n, narr, x, y, a, ax, ay), x.size)
+        g, r = yg.reshape(lines, nproc), yo.reshape(lines, nproc)
+        err = np.abs(g - r).max(axis=1)
+        assert np.all(err <= TOL * np.abs(r).max(axis=1)), (op, nproc, a, ax, ay)
+
+
 @pytest.mark.parametrize('bc', [0, 1, -1, 2])
 @pytest.mark.parametrize('idim', [0, 1, 2])
 def test_kinetic1d_dotin(pkg, O, bc, idim):
