@@ -211,15 +211,18 @@ def test_magicfilter3d_lines_keep_their_own_scale(pkg, O):
 
 @pytest.mark.parametrize('narr', [1, 2])
 def test_magicfilter3d_exponent_handoff_matches_separate_sweeps(pkg, narr):
-    """On 128 x 128 x 32 grids each exact MagicFilter3D sweep hands the next one
+    """On 128 x 64 x 32 grids each exact MagicFilter3D sweep hands the next one
     its line exponents from the epilogue (every tile column holds whole lines
-    of the next sweep: 128 of them after the first sweep, 4 x 32 after the
+    of the next sweep: 2 x 64 after the first sweep, 4 x 32 after the
     second).  The exact products depend only on each line's exponent, so the
-    result must equal three 1D MagicFilter sweeps, each with its own exponent
-    pass, bit for bit; the input's magnitude steps by 2^40 along axis 2 (every
-    line of the second sweep has its own scale)."""
+    result must equal three 1D MagicFilter sweeps bit for bit: the first (128
+    contiguous periodic points) takes its tile windows' exponents like the
+    first MagicFilter3D sweep, the other two (64 and 32 points, shorter than a
+    tile window) make their own line-exponent pass.  The input's magnitude
+    steps by 2^40 along axis 2 (every line of the second sweep has its own
+    scale).  The hand-off to 128-point lines runs in the full-size tests."""
     from boast_lig_gb300 import inputs
-    n = [128, 128, 32]
+    n = [128, 64, 32]
     N = int(np.prod(n))
     x = inputs.uniform(907, N * narr).reshape(narr, n[2], n[1], n[0])
     x = (x * (2.0 ** (40 * (np.arange(n[2]) % 3 - 1)))[None, :, None, None]).ravel()

@@ -117,28 +117,34 @@ def test_wavelet1d_periodic_long_lines(pkg, O, op, nproc, idim):
 
 @pytest.mark.parametrize('op', CONV_OPS)
 @pytest.mark.parametrize('nproc', [80, 97, 130, 203])
-def test_conv1d_periodic_long_contiguous_lines(pkg, O, op, nproc):
-    """Contiguous periodic lines at least one tile window long (80 input
-    elements for 16 taps, 96 for 29): the exact sweep takes each tile
-    window's largest exponent in its producers instead of a pass over the
-    array (80 with 29 taps stays below the window and keeps the pass).
-    Lengths not a multiple of 4 put the wrap inside the 8-element groups.
-    Every line has its own magnitude (2^-40, 1, 2^40) and magnitudes also step
-    by 2^20 along each line, so the tile windows of one line get different
-    scales; each line must match the oracle to 1e-13 of its largest output."""
-    n = [nproc, 6, 5]
+@pytest.mark.parametrize('idim', [0, 1, 2])
+def test_conv1d_periodic_long_lines(pkg, O, op, nproc, idim):
+    """Periodic lines at least one tile window long (80 input elements for 16
+    taps, 96 for 29), contiguous (idim 0) or strided: the exact sweep takes
+    each tile window's largest exponent in its producers instead of a pass
+    over the array (80 with 29 taps stays below the window and keeps the
+    pass).  Lengths not a multiple of 4 put the wrap inside the 8-element
+    groups.  Every line has its own magnitude (2^-40, 1, 2^40) and magnitudes
+    also step by 2^20 along each line, so the tile windows of one line get
+    different scales; each line must match the oracle to 1e-13 of its largest
+    output."""
+    n = [6, 5, 4]
+    n[idim] = nproc
     narr = 2
-    lines = n[1] * n[2] * narr
-    x = seeded(700 + nproc, nproc * lines).reshape(lines, nproc)
-    line_scale = 2.0 ** (40 * (np.arange(lines) % 3 - 1))
+    shape = (narr, n[2], n[1], n[0])
+    ax = 3 - idim                                    # the line's axis in C order
+    x = np.moveaxis(seeded(700 + nproc + 7 * idim, int(np.prod(shape))).reshape(shape), ax, -1)
+    lines = x.shape[:-1]
+    line_scale = 2.0 ** (40 * (np.arange(int(np.prod(lines))).reshape(lines) % 3 - 1))
     along = 2.0 ** (20 * ((np.arange(nproc) // 48) % 2))
-    x = (x * line_scale[:, None] * along[None, :]).ravel()
-    for (a, ax, ay) in [(1.0, 0.0, 0.0), (0.7, -0.3, 1.5)]:
+    x = np.ascontiguousarray(np.moveaxis(x * line_scale[..., None] * along, -1, ax)).ravel()
+    for (a, a_x, a_y) in [(1.0, 0.0, 0.0), (0.7, -0.3, 1.5)]:
         y = seeded(800 + nproc, x.size)
-        yg, yo = run_both(pkg, O, op, (3, 0, n, 0, n, n, narr, x, y, a, ax, ay), x.size)
-        g, r = yg.reshape(lines, nproc), yo.reshape(lines, nproc)
+        yg, yo = run_both(pkg, O, op, (3, idim, n, 0, n, n, narr, x, y, a, a_x, a_y), x.size)
+        g = np.moveaxis(yg.reshape(shape), ax, -1).reshape(-1, nproc)
+        r = np.moveaxis(yo.reshape(shape), ax, -1).reshape(-1, nproc)
         err = np.abs(g - r).max(axis=1)
-        assert np.all(err <= TOL * np.abs(r).max(axis=1)), (op, nproc, a, ax, ay)
+        assert np.all(err <= TOL * np.abs(r).max(axis=1)), (op, nproc, idim, a, a_x, a_y)
 
 
 @pytest.mark.parametrize('bc', [0, 1, -1, 2])
