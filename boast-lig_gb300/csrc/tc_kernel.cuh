@@ -17,9 +17,10 @@
 //   * the filter, with the operator scalar a folded in exactly (128-bit
 //     product of the two mantissas), is cut the same way into e_0..e_7;
 //   * byte-pair products are at most 2^14 in magnitude and every partial
-//     sum over <= 32 products x 8 pairs stays within 2^22, so FP32
-//     accumulation in TMEM is exact and every accumulator converts to an
-//     integer with one FP32 add;
+//     sum over <= 32 products x 8 pairs stays within 2^22; every TMEM
+//     accumulator starts at 1.5 * 2^23 (one MMA of a constant tile per output
+//     block), so all its values are integers in [2^23, 2^24], where FP32 is
+//     exact, and its bits are 0x4B400000 plus the sum;
 //   * the 36 pairs of order k = s + t <= 7 are accumulated, one TMEM
 //     accumulator per order; the epilogue recombines
 //     Y = sum_k Acc_k 2^(46-8k) in int64 (the orders 6-7 rounded to an
@@ -101,9 +102,13 @@ template <int KIND, int NT, int SCH> struct Geom {
     static constexpr int A_BYTES = NS * A_SLICE;
     static constexpr int KBP = KB * PL;                          // K of a block window
     static constexpr int B_BYTES = BN * KBP * ESZ;
+    // exact scheme: a 128 x 16 FP16 tile holding 2048 at K = 0, 1, 2 of every
+    // row; as both operands of an N = 128 MMA it sets an output block's eight
+    // order accumulators to 3 * 2048^2 = 1.5 * 2^23
+    static constexpr int Z_BYTES = SCH == SCH_EXACT ? kM * 16 * 2 : 0;
     static constexpr int AUX = 1024 + 3 * 4 * kM + 2 * 4 * 32 * 4;   // barriers, slots, row exponents,
                                                                  // next-sweep column maxima
-    static constexpr int SMEM = A_BYTES + B_BYTES + AUX + 1024;
+    static constexpr int SMEM = A_BYTES + B_BYTES + Z_BYTES + AUX + 1024;
     static constexpr int HALF_COLS = 2 * ORD * 16;               // one TMEM half (2 blocks)
     static constexpr uint32_t TMEM_COLS = 2 * HALF_COLS <= 32 ? 32 : 2 * HALF_COLS <= 64 ? 64 : 2 * HALF_COLS <= 128 ? 128 : 2 * HALF_COLS <= 256 ? 256 : 512;
     static_assert(2 * HALF_COLS <= 512, "TMEM columns");
@@ -260,15 +265,9 @@ __device__ __forceinline__ double ll_scaled_fast(long long Y, int se, bool &bad)
     return Y == 0 ? 0.0 : __longlong_as_double((long long)bits);
 }
 
-// Bits of an FP32 accumulator plus 1.5 * 2^23: the integer value v of the
-// accumulator (|v| <= 2^22 by the digit bounds) sits in the low mantissa bits,
-// biased: bits = 0x4B400000 + v.
-__device__ __forceinline__ uint32_t acc_bits(uint32_t u) {
-    return __float_as_uint(__uint_as_float(u) + 12582912.0f);
-}
-
 // Y = sum_k Acc_k 2^(46 - 8k) over the 8 order accumulators of one output,
-// from their biased bits b_k = Acc_k + 0x4B400000 (acc_bits): orders 0-5 by
+// from their biased bits b_k = Acc_k + 0x4B400000 (the bits of an FP32
+// accumulator that started at 1.5 * 2^23, |Acc_k| <= 2^22): orders 0-5 by
 // Horner modulo 2^64 (three 32x32+64 multiply-adds for the low terms, a
 // 32-bit add into the high word for the two top terms), orders 6-7 as the
 // nearest integer of Acc_6 / 4 + Acc_7 / 1024 (one 32-bit multiply-add and
@@ -369,19 +368,25 @@ __device__ __forceinline__ void split_f32(uint32_t f, uint32_t (&h)[SPLITS]) {
 // contiguous in TMEM, so ONE MMA per data plane s covers all its pairs:
 // D = columns 16s.. of the block, N = 16 (ORD - s) (a prefix of the stacked
 // filter), giving pair (s, t) at order s + t.  The s = 0 MMA of the first K
-// step initialises every order.  Output block j starts 16 elements into the A
-// planes; one MMA covers 32 bytes of K (two core matrices).  Descriptors are
-// advanced by adding the (16-byte unit) offset to the start-address field
-// (addresses < 256 KB never carry out of it).
+// step initialises every order (split schemes); in the exact scheme one MMA of
+// the constant tile (z_desc, N = 128) first sets all eight orders of the block
+// to 1.5 * 2^23 and every data MMA accumulates.  Output block j starts 16
+// elements into the A planes; one MMA covers 32 bytes of K (two core
+// matrices).  Descriptors are advanced by adding the (16-byte unit) offset to
+// the start-address field (addresses < 256 KB never carry out of it).
 template <int KIND, int NT, int SCH, int H>
-__device__ __forceinline__ void issue_half(uint32_t tmem, uint64_t a_desc0, uint64_t b_desc0) {
+__device__ __forceinline__ void issue_half(uint32_t tmem, uint64_t a_desc0, uint64_t b_desc0,
+                                           uint64_t z_desc) {
     using G = Geom<KIND, NT, SCH>;
     constexpr bool TF = SCH == SCH_TF32X3;
+    constexpr bool EX = SCH == SCH_EXACT;
     constexpr int NKS = G::KBP / G::MK;
 #pragma unroll
     for (int jj = 0; jj < 2; ++jj) {
         const int j = 2 * H + jj;
         const int a_blk = (16 * G::PL / G::CE) * j * 2048;
+        if (EX) mma<false>(tmem + (uint32_t)(H * G::HALF_COLS + jj * G::ORD * 16), z_desc, z_desc,
+                           G::idesc(16 * G::ORD), 0u);
 #pragma unroll
         for (int sl = 0; sl < G::NS; ++sl) {
             const int sd = sl * G::PL;                           // first plane (order) of the slice
@@ -391,7 +396,7 @@ __device__ __forceinline__ void issue_half(uint32_t tmem, uint64_t a_desc0, uint
             for (int ks = 0; ks < NKS; ++ks) {
                 const uint64_t ad = a_desc0 + (uint64_t)((sl * G::A_SLICE + a_blk + 2 * ks * 2048) >> 4);
                 const uint64_t bd = b_desc0 + (uint64_t)((2 * ks * G::LBO_B) >> 4);
-                mma<TF>(d, ad, bd, id, (sl == 0 && ks == 0) ? 0u : 1u);
+                mma<TF>(d, ad, bd, id, (EX || sl > 0 || ks > 0) ? 1u : 0u);
             }
         }
     }
@@ -461,7 +466,8 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *A = smem;
     uint8_t *B = smem + G::A_BYTES;
-    uint8_t *aux = B + G::B_BYTES;
+    uint8_t *Z = B + G::B_BYTES;                      // exact scheme: accumulator bias tile
+    uint8_t *aux = Z + G::Z_BYTES;
     uint64_t *bars = (uint64_t *)aux;                 // 9 barriers (16 slots)
     uint32_t *tslot = (uint32_t *)(aux + 128);
     int *rowE3 = (int *)(aux + 1024);                 // row exponents, by tile index mod 3
@@ -518,6 +524,12 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
         if (G::ESZ == 4) *(uint32_t *)b = v;
         else *(unsigned short *)b = (unsigned short)v;
     }
+    // bias tile, K-major core matrices like A: (row, k) at (k / 8) * 2048 +
+    // (row / 8) * 128 + (row % 8) * 16 + (k % 8) * 2; FP16 2048 = 0x6800
+    for (int idx = tid; idx < G::Z_BYTES / 2; idx += kThreads) {
+        const int k8 = idx / 1024, rem = idx % 1024, k = rem % 8;
+        ((unsigned short *)Z)[idx] = (k8 == 0 && k < 3) ? (unsigned short)0x6800 : (unsigned short)0;
+    }
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
@@ -527,6 +539,7 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
 
     const uint64_t a_desc0 = umma_desc(saddr(A), 2048, 128);
     const uint64_t b_desc0 = umma_desc(saddr(B), G::LBO_B, 128);
+    const uint64_t z_desc = umma_desc(saddr(Z), 2048, 128);
     if (warp < kProducers / 32) {
         // ============ producers: thread = (row, half of every chunk pair);
         // half-warps cover 16 consecutive rows.  The KT elements of a row are
@@ -823,8 +836,8 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
             if (ew == 4 * hf) {
                 if (lane == 0) {
                     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                    if (hf == 0) issue_half<KIND, NT, SCH, 0>(tmem, a_desc0, b_desc0);
-                    else issue_half<KIND, NT, SCH, 1>(tmem, a_desc0, b_desc0);
+                    if (hf == 0) issue_half<KIND, NT, SCH, 0>(tmem, a_desc0, b_desc0, z_desc);
+                    else issue_half<KIND, NT, SCH, 1>(tmem, a_desc0, b_desc0, z_desc);
                     commit(bT_full[hf]);
                     if (hf == 0) commit(pfree0);
                     commit(pfree12);
@@ -903,9 +916,9 @@ sweep_tc_kernel(const __grid_constant__ Sweep S0, const __grid_constant__ TcFilt
                     long long Y[8];
 #pragma unroll
                     for (int i = 0; i < 8; ++i) {
-                        uint32_t bb[G::ORD];
+                        uint32_t bb[G::ORD];              // 0x4B400000 + Acc_k (biased start)
 #pragma unroll
-                        for (int k = 0; k < G::ORD; ++k) bb[k] = acc_bits(acc[k][i]);
+                        for (int k = 0; k < G::ORD; ++k) bb[k] = acc[k][i];
                         Y[i] = horner_bal<G::ORD>(bb);
                     }
 #pragma unroll

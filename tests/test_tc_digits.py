@@ -5,8 +5,9 @@ folded in) to signed 62-bit integers (data truncated toward zero, filter
 rounded), cuts each into 8 balanced byte digits in [-128, 127] held exactly
 in FP16 (the bytes of X + 0x8080808080808080 minus 128), accumulates the
 36 digit pairs of order k = s + t <= 7 in one FP32 accumulator per order
-(exact while every partial sum stays within 2^22, which also makes the
-accumulator an integer after one FP32 add of 1.5 * 2^23), and recombines
+that starts at 1.5 * 2^23 (exact while every partial sum stays within
+2^22: every value is then an integer in [2^23, 2^24], whose FP32 bits are
+0x4B400000 plus the sum), and recombines
 Y = sum_{k<=5} Acc_k 2^(46-8k) + round(Acc_6 / 4 + Acc_7 / 1024) in int64.
 This test replays that arithmetic with exact integers on the kinetic and
 MagicFilter filters, checks the 2^22 bound the exactness rests on and the
@@ -140,11 +141,19 @@ def test_digit_arithmetic_matches_oracle(O, pkg, which):
 def test_accumulator_bound_is_tight_for_32_products():
     """The largest filter (32 products per output: the MagicFilter-combined
     wavelets) with every digit at -128 reaches exactly 2^22 in order 7,
-    where the one-add integer conversion still holds: 1.5 * 2^23 + v is
-    exact for |v| <= 2^22 and its bits are 0x4B400000 + v."""
+    where the biased accumulator still holds: 1.5 * 2^23 + v is exact for
+    |v| <= 2^22 and its bits are 0x4B400000 + v.  The start value comes from
+    one MMA of a constant tile with 2048 (exact in FP16) at three K
+    positions, as both operands: 3 * 2048^2 = 1.5 * 2^23."""
     v = 8 * 32 * 128 * 128
     assert v == 2 ** 22
+    assert float(np.float16(2048.0)) == 2048.0
+    assert int(np.array(2048.0, dtype=np.float16).view(np.uint16)) == 0x6800
+    start = np.float32(0)
+    for _ in range(3):
+        start = np.float32(start + np.float32(2048.0) * np.float32(2048.0))
+    assert float(start) == 1.5 * 2 ** 23
     for t in (-v, -v + 1, -1, 0, 1, v - 1, v):
-        f = np.float32(1.5 * 2 ** 23) + np.float32(t)
+        f = start + np.float32(t)
         assert float(f) == 1.5 * 2 ** 23 + t
         assert int(f.view(np.uint32)) == 0x4B400000 + t
