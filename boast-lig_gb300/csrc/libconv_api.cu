@@ -139,11 +139,12 @@ struct PipeSlot {
     DevBuf buf[4];                   // x, y, w1, w2 of one chunk
     DevBuf scratch, lineexp;
 };
-// Chunks per host-pointer call and streams they rotate over: 16 chunks on 8
-// streams keep both copy directions busy; the first chunk's copy-in and the
-// last chunk's sweeps and copy-out run alone, so smaller chunks shorten them
-// (32 x 128^3 MagicFilter3D + Kinetic3D from pinned buffers: 8 chunks on 3
-// streams 8.74 Gpts/s, 16 on 8 9.04; 4-5 streams sometimes 7.9).
+// Chunks per host-pointer call (at most; each at least 48 MB in and out) and
+// streams they rotate over: 16 chunks on 8 streams keep both copy directions
+// busy; the first chunk's copy-in and the last chunk's sweeps and copy-out run
+// alone, so smaller chunks shorten them (32 x 128^3 MagicFilter3D + Kinetic3D
+// from pinned buffers: 8 chunks on 3 streams 8.74 Gpts/s, 16 on 8 9.04; 4-5
+// streams sometimes 7.9).
 constexpr int kPipeChunks = 16;
 constexpr int kPipeSlots = 8;
 
@@ -705,7 +706,9 @@ int exec_host_pipelined(const Plan &P, int narr, const double *x, double *y, Dev
     const size_t xs = P.elems[B_X] / narr, ys = P.elems[B_Y] / narr;
     const size_t per = (xs + ys) * sizeof(double);
     int c = (narr + kPipeChunks - 1) / kPipeChunks;
-    while ((size_t)c * per < (1u << 20) && c < narr) ++c;   // at least 1 MB per chunk
+    // at least 48 MB in and out per chunk: smaller chunks leave the host's
+    // per-chunk launches comparable to their copies
+    while ((size_t)c * per < (48u << 20) && c < narr) ++c;
     const int nchunk = (narr + c - 1) / c, rem = narr - (nchunk - 1) * c;
     const Plan Qc = with_narr(P, narr, c), Qr = with_narr(P, narr, rem);
     int rc;
