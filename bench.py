@@ -147,9 +147,10 @@ class MfKin128:
     ops = ('magicfilter3d', 'kinetic3d')
     a = [-0.5 / HGRID ** 2] * 3
     launches = 6                                     # 3 sweeps per operator
-    # exact tensor-core mode: a line-exponent pass before each MagicFilter sweep, one shared
-    # pass over x for the three kinetic sweeps
-    exact_prepasses = 4
+    # exact tensor-core mode: one shared line-exponent pass over x for the three kinetic
+    # sweeps; the first MagicFilter sweep takes its tile windows' exponents itself and hands
+    # the next sweep its line exponents, which hands them on to the third
+    exact_prepasses = 1
     desc = ('{B} grids of 128^3 periodic per GPU per step: MagicFilter3D (d_sfrf_ld_narr) + '
             'Kinetic3D (d_kin_narr, h=0.45)')
 
@@ -1460,7 +1461,10 @@ def run_poisson(args, W):
             'step': {'algorithmic_bytes_per_point': W.bytes_per_pt,
                      'achieved_gbs': W.bytes_per_pt * N / step_s / 1e9,
                      'frac': W.bytes_per_pt * N / step_s / 1e9 / pk['hbm']}}
-    launches = {'tc_exact': 15, 'fp64': 9}.get(args.mode, 9)
+    # six sweeps, the edge kernels of the two sweeps along the non-periodic axis and the cc
+    # kernel; in the exact mode those two sweeps also make a line-exponent pass (the four
+    # periodic ones take their tile windows' exponents themselves)
+    launches = {'tc_exact': 11, 'fp64': 9}.get(args.mode, 9)
     exact = args.mode in ('fp64', 'tc_exact')
     line = {'metric': W.metric, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
             'warmup': max(args.warmup, 3), 'ms_per_step': ms / args.steps,
