@@ -151,6 +151,10 @@ class MfKin128:
     # sweeps; the first MagicFilter sweep takes its tile windows' exponents itself and hands
     # the next sweep its line exponents, which hands them on to the third
     exact_prepasses = 1
+    # the whole step's algorithmic bytes per grid point: as separate sweeps (MagicFilter 3 x 16;
+    # kinetic 16 + 24 + 24, its y and z sweeps reading x beside their partial sum) and with x
+    # read once and both outputs written once (the floor of any fusion of the two operators)
+    step_bytes = {'sweeps': 48.0 + 64.0, 'fused': 24.0}
     desc = ('{B} grids of 128^3 periodic per GPU per step: MagicFilter3D (d_sfrf_ld_narr) + '
             'Kinetic3D (d_kin_narr, h=0.45)')
 
@@ -1624,6 +1628,8 @@ def run_gpu(args):
             'frac': achieved / pk['hbm'], 'traffic': traffic, 'kernel': W.dom_kernel[args.mode],
             'peak_source': pk['source'],
             'algorithmic_bytes_per_point': W.dom_bytes_per_pt}
+    if getattr(W, 'step_bytes', None):
+        roof['step'] = step_roofline(W.step_bytes, B * Ni, ms / 1e3 / args.steps, pk['hbm'])
     if args.mode != 'fp64':
         # MMA work per output point (not algorithmic flops): products x K x 2
         prods = {'tc_exact': W.pairs_exact, 'tc_bf16x3': 6, 'tc_tf32x3': 3}[args.mode]
@@ -1673,6 +1679,17 @@ def run_gpu(args):
         print(json.dumps(line), flush=True)
     R.close()
     return line
+
+
+def step_roofline(step_bytes, points, step_s, hbm_gbs):
+    """The whole step against HBM for each byte count of step_bytes
+    ({name: algorithmic bytes per point}): GB/s over `points` grid points per
+    step of `step_s` seconds, and the fraction of `hbm_gbs`."""
+    out = {}
+    for name, v in step_bytes.items():
+        gbs = v * points / step_s / 1e9
+        out[name] = {'algorithmic_bytes_per_point': v, 'achieved_gbs': gbs, 'frac': gbs / hbm_gbs}
+    return out
 
 
 def sub_records(args):
